@@ -1,0 +1,226 @@
+"""coupe_gb300 — coupe's Rcb and Rib on a GB300 GPU.
+
+Python mirror of coupe's partitioning interface for these two algorithms
+(coupe/src/lib.rs:76-91 `Partition`, coupe/src/algorithms/recursive_bisection.rs
+:780-812 `Rcb` and :902-930 `Rib`), calling the C ABI of libcoupe_gpu.so
+(include/coupe.h, include/coupe_gpu.h) through ctypes.  There is no CPU
+fallback: every call runs the CUDA engine, and loading fails loudly when the
+library has not been built.
+
+    import numpy as np, coupe_gb300 as coupe
+    ids = np.zeros(len(points), dtype=np.uint64)
+    coupe.Rcb(iter_count=10, tolerance=0.01).partition(ids, (points, weights))
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+__all__ = [
+    "Rcb", "Rib", "CoupeError", "lib", "library_path", "MODES", "last_stats",
+    "rcb_device", "rib_device", "rib_matrix_device",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(_HERE, "libcoupe_gpu.so")
+
+# enum coupe_err / coupe_type / coupe_gpu_mode (include/coupe.h, coupe_gpu.h)
+ERR_OK, ERR_ALLOC, ERR_CRASH, ERR_BAD_DIMENSION, ERR_BAD_TYPE, ERR_BIPART_ONLY, \
+    ERR_LEN_MISMATCH, ERR_NOT_FOUND, ERR_NEG_VALUES = range(9)
+COUPE_INT, COUPE_INT64, COUPE_DOUBLE = 0, 1, 2
+MODES = {"ref32": 0, "f64": 1, "f32key_f64band": 2}
+
+# Symbols the library exports (checked by the CPU test-suite).
+EXPORTED = [
+    "coupe_strerror", "coupe_data_free", "coupe_data_array", "coupe_data_constant",
+    "coupe_data_fn", "coupe_rcb", "coupe_rib",
+    "coupe_gpu_rcb", "coupe_gpu_rib", "coupe_gpu_rcb_device", "coupe_gpu_rib_device",
+    "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
+]
+
+
+class CoupeError(RuntimeError):
+    def __init__(self, code, detail=""):
+        self.code = code
+        msg = lib().coupe_strerror(code).decode()
+        if detail:
+            msg += " (" + detail + ")"
+        super().__init__(msg)
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "points", "levels", "splits", "split_steps", "max_split_steps", "hist_passes",
+        "hist_points", "band_points", "kernel_launches", "algo_bytes")] + [
+        ("root_weight_sum", ctypes.c_double), ("device_ms", ctypes.c_double),
+        ("fixed_scale", ctypes.c_int), ("mode", ctypes.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+I_TH = ctypes.CFUNCTYPE(ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t)
+_lib = None
+
+
+def lib():
+    """Loads libcoupe_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(library_path):
+        raise ImportError("libcoupe_gpu.so not built: run `python coupe_gb300/build.py` "
+                          "or __graft_entry__.build()")
+    L = ctypes.CDLL(library_path)
+    vp, u64, dbl, i32 = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_int
+    L.coupe_strerror.argtypes = [i32]
+    L.coupe_strerror.restype = ctypes.c_char_p
+    L.coupe_data_free.argtypes = [vp]
+    L.coupe_data_free.restype = None
+    L.coupe_data_array.argtypes = [u64, i32, vp]
+    L.coupe_data_array.restype = vp
+    L.coupe_data_constant.argtypes = [u64, i32, vp]
+    L.coupe_data_constant.restype = vp
+    L.coupe_data_fn.argtypes = [vp, u64, i32, I_TH]
+    L.coupe_data_fn.restype = vp
+    for f in (L.coupe_rcb, L.coupe_rib):
+        f.argtypes = [vp, u64, vp, vp, u64, dbl]
+        f.restype = i32
+    for f in (L.coupe_gpu_rcb, L.coupe_gpu_rib):
+        f.argtypes = [vp, u64, vp, vp, u64, dbl, i32]
+        f.restype = i32
+    L.coupe_gpu_rcb_device.argtypes = [vp, u64, u64, vp, i32, vp, u64, dbl, i32, vp, vp]
+    L.coupe_gpu_rcb_device.restype = i32
+    L.coupe_gpu_rib_device.argtypes = [vp, u64, u64, vp, i32, vp, u64, dbl, i32, vp]
+    L.coupe_gpu_rib_device.restype = i32
+    L.coupe_gpu_rib_matrix.argtypes = [u64, u64, vp, vp, vp]
+    L.coupe_gpu_rib_matrix.restype = i32
+    L.coupe_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
+    L.coupe_gpu_last_stats.restype = None
+    L.coupe_gpu_last_error.argtypes = []
+    L.coupe_gpu_last_error.restype = ctypes.c_char_p
+    L.coupe_gpu_version.argtypes = []
+    L.coupe_gpu_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def last_stats():
+    s = Stats()
+    lib().coupe_gpu_last_stats(ctypes.byref(s))
+    return s.as_dict()
+
+
+def _check(rc):
+    if rc != ERR_OK:
+        raise CoupeError(rc, lib().coupe_gpu_last_error().decode())
+
+
+def _weight_type(w):
+    if w.dtype == np.int32:
+        return COUPE_INT
+    if w.dtype == np.int64:
+        return COUPE_INT64
+    if w.dtype == np.float64:
+        return COUPE_DOUBLE
+    raise TypeError("weights must be int32, int64 or float64, got %s" % w.dtype)
+
+
+def _as_weights(weights, n):
+    if np.isscalar(weights):
+        weights = np.full(n, weights)
+    w = np.asarray(weights)
+    if w.dtype.kind in "iu" and w.dtype not in (np.int32,):
+        w = w.astype(np.int64)
+    elif w.dtype.kind == "f":
+        w = w.astype(np.float64)
+    return np.ascontiguousarray(w)
+
+
+@dataclass
+class _Bisection:
+    iter_count: int = 0
+    tolerance: float = 0.0
+    mode: str = "ref32"
+    _rib = False
+
+    def partition(self, part_ids, data):
+        """Writes one part id per point into `part_ids` (uint64, length N).
+
+        data = (points, weights): points is an (N, D) array of float64 with
+        D in {2, 3}; weights an array of N int32/int64/float64 values (a
+        scalar is repeated).  Mirrors Partition::partition.
+        """
+        points, weights = data
+        p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+        if p.ndim != 2:
+            raise ValueError("points must be an (N, D) array")
+        n, dim = p.shape
+        w = _as_weights(weights, n)
+        if part_ids.dtype != np.uint64 or not part_ids.flags.c_contiguous:
+            raise TypeError("part_ids must be a contiguous uint64 array")
+        if len(part_ids) != n:
+            raise CoupeError(ERR_LEN_MISMATCH)
+        L = lib()
+        dp = L.coupe_data_array(n, COUPE_DOUBLE, p.ctypes.data)
+        dw = L.coupe_data_array(len(w), _weight_type(w), w.ctypes.data)
+        try:
+            fn = L.coupe_gpu_rib if self._rib else L.coupe_gpu_rcb
+            rc = fn(part_ids.ctypes.data, dim, dp, dw, self.iter_count, self.tolerance, MODES[self.mode])
+        finally:
+            L.coupe_data_free(dp)
+            L.coupe_data_free(dw)
+        _check(rc)
+
+
+class Rcb(_Bisection):
+    """Recursive coordinate bisection (coupe::Rcb): at most 2**iter_count parts."""
+
+
+class Rib(_Bisection):
+    """Recursive inertial bisection (coupe::Rib): Rcb after aligning the first
+    axis with the points' principal inertia axis."""
+    _rib = True
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def rcb_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", matrix=None, stream=None):
+    """Rcb on CUDA tensors (torch): part_ids int64/uint64 (N,), points float64
+    (N, D) contiguous, weights int32/int64/float64 (N,).  `matrix` (D x D)
+    applies p -> matrix @ p first.  Synchronises the stream before returning."""
+    import torch
+    n, dim = points.shape
+    wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+    m = None
+    if matrix is not None:
+        m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float64).reshape(dim, dim))
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_rcb_device(_ptr(part_ids), n, dim, _ptr(points), wt, _ptr(weights), iter_count,
+                                    tolerance, MODES[mode], m.ctypes.data if m is not None else None,
+                                    ctypes.c_void_p(s))
+    _check(rc)
+
+
+def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None):
+    """Rib on CUDA tensors (see rcb_device)."""
+    import torch
+    n, dim = points.shape
+    wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_rib_device(_ptr(part_ids), n, dim, _ptr(points), wt, _ptr(weights), iter_count,
+                                    tolerance, MODES[mode], ctypes.c_void_p(s))
+    _check(rc)
+
+
+def rib_matrix_device(points, stream=None):
+    """The Rib basis change (obb_to_aabb) of CUDA float64 points (N, D)."""
+    import torch
+    n, dim = points.shape
+    out = np.zeros((dim, dim), dtype=np.float64)
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _check(lib().coupe_gpu_rib_matrix(n, dim, _ptr(points), out.ctypes.data, ctypes.c_void_p(s)))
+    return out

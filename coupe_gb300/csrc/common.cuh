@@ -1,0 +1,290 @@
+// Shared device/host definitions of the GB300 Rcb/Rib engine: key and weight
+// arithmetic, the 128-bit fixed-point weight sums, ordered encodings for
+// atomic min/max, and the per-segment record of a tree level.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstring>
+
+#define CG_HD __host__ __device__ __forceinline__
+
+namespace cg {
+
+// ---------------------------------------------------------------------------
+// Ordered unsigned encodings: a < b (IEEE, non-NaN) iff enc(a) < enc(b).
+// -0.0 encodes just below +0.0.
+// ---------------------------------------------------------------------------
+CG_HD uint32_t ord_f32(float f) {
+#ifdef __CUDA_ARCH__
+    uint32_t b = __float_as_uint(f);
+#else
+    uint32_t b;
+    memcpy(&b, &f, 4);
+#endif
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+CG_HD float unord_f32(uint32_t u) {
+    uint32_t b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+CG_HD uint64_t ord_f64(double f) {
+#ifdef __CUDA_ARCH__
+    uint64_t b = (uint64_t)__double_as_longlong(f);
+#else
+    uint64_t b;
+    memcpy(&b, &f, 8);
+#endif
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+CG_HD double unord_f64(uint64_t u) {
+    uint64_t b = (u & 0x8000000000000000ull) ? (u & 0x7fffffffffffffffull) : ~u;
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double f;
+    memcpy(&f, &b, 8);
+    return f;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Key precision.  KeyF32 is coupe's arithmetic (f32 keys, `(min + max) / 2.0`
+// in f32, f32 distances); KeyF64 the same algorithm in f64.
+// ---------------------------------------------------------------------------
+struct KeyF32 {
+    typedef float T;
+    typedef uint32_t Ord;
+    static constexpr Ord ORD_INF = 0xff800000u;  // ord_f32(+inf)
+    CG_HD static Ord ord(T k) { return ord_f32(k); }
+    CG_HD static T unord(Ord u) { return unord_f32(u); }
+    CG_HD static T from_f64(double v) { return (float)v; }
+    CG_HD static T inf() { return unord_f32(ORD_INF); }
+    // recursive_bisection.rs:472 — (min + max) / 2.0 in f32
+    CG_HD static T mid(T a, T b) { return (a + b) / 2.0f; }
+};
+struct KeyF64 {
+    typedef double T;
+    typedef uint64_t Ord;
+    static constexpr Ord ORD_INF = 0xfff0000000000000ull;  // ord_f64(+inf)
+    CG_HD static Ord ord(T k) { return ord_f64(k); }
+    CG_HD static T unord(Ord u) { return unord_f64(u); }
+    CG_HD static T from_f64(double v) { return v; }
+    CG_HD static T inf() { return unord_f64(ORD_INF); }
+    CG_HD static T mid(T a, T b) { return (a + b) / 2.0; }
+};
+
+// ---------------------------------------------------------------------------
+// 128-bit fixed-point sums of f64 weights.  For n weights whose largest
+// magnitude A satisfies 2^(e-1) <= A < 2^e, the scale is
+// s = 126 - e - ceil(log2 n); each weight becomes q = round_half_even(w 2^s)
+// as a two's-complement 128-bit integer, so that any sum of at most n terms
+// stays below 2^126 in magnitude and integer addition makes every sum
+// independent of its order.  A sum Q is read back as an f64 by rounding |Q|
+// to 53 significant bits (half to even) and scaling by 2^-s.
+// ---------------------------------------------------------------------------
+CG_HD int ceil_log2_u64(uint64_t n) {
+    int l = 0;
+    while (l < 63 && (1ull << l) < n) ++l;
+    return l;
+}
+
+CG_HD int fixed_scale_from_max(double amax, uint64_t n) {
+    if (!(amax > 0.0)) return 0;
+    int e;
+    frexp(amax, &e);
+    return 126 - e - ceil_log2_u64(n);
+}
+
+CG_HD unsigned __int128 fixed_q_bits(double w, int s) {
+    if (w == 0.0) return 0;
+    int ex;
+    double f = frexp(fabs(w), &ex);
+    uint64_t m = (uint64_t)ldexp(f, 53);  // exact, 2^52 <= m < 2^53
+    int x = ex - 53 + s;
+    unsigned __int128 q;
+    if (x >= 0) {
+        q = (unsigned __int128)m << x;
+    } else {
+        int r = -x;
+        if (r >= 54) {
+            q = 0;
+        } else {
+            uint64_t qi = m >> r;
+            uint64_t rem = m & ((1ull << r) - 1);
+            uint64_t half = 1ull << (r - 1);
+            if (rem > half || (rem == half && (qi & 1))) ++qi;
+            q = qi;
+        }
+    }
+    return w < 0 ? (unsigned __int128)0 - q : q;
+}
+
+CG_HD int clz128(unsigned __int128 a) {
+    uint64_t hi = (uint64_t)(a >> 64), lo = (uint64_t)a;
+#ifdef __CUDA_ARCH__
+    return hi ? __clzll((long long)hi) : 64 + __clzll((long long)lo);
+#else
+    return hi ? __builtin_clzll(hi) : (lo ? 64 + __builtin_clzll(lo) : 128);
+#endif
+}
+
+CG_HD double fixed_to_f64(unsigned __int128 Qbits, int s) {
+    if (Qbits == 0) return 0.0;
+    bool neg = (Qbits >> 127) != 0;
+    unsigned __int128 a = neg ? (unsigned __int128)0 - Qbits : Qbits;
+    int hb = 127 - clz128(a);
+    uint64_t m;
+    int x = 0;
+    if (hb <= 52) {
+        m = (uint64_t)a;
+    } else {
+        int sh = hb - 52;
+        m = (uint64_t)(a >> sh);
+        unsigned __int128 rem = a & (((unsigned __int128)1 << sh) - 1);
+        unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        if (rem > half || (rem == half && (m & 1))) ++m;
+        if (m == (1ull << 53)) {
+            m >>= 1;
+            ++sh;
+        }
+        x = sh;
+    }
+    double r = ldexp((double)m, x - s);
+    return neg ? -r : r;
+}
+
+// ---------------------------------------------------------------------------
+// Weight arithmetic (coupe's RcbWeight, recursive_bisection.rs:708-722, with
+// release-build wrapping for integers).  Sums are accumulated in LIMBS
+// unsigned 64-bit words so that atomics can add them in any order:
+//   int32:  one word, the low 32 bits are the wrapped i32 sum;
+//   int64:  one word, the wrapped i64 sum;
+//   double: four words holding 32-bit chunks of the 128-bit fixed-point q,
+//           recombined with carries (exact while fewer than 2^32 terms).
+// V values travel through the segment table as 64 raw bits.
+// ---------------------------------------------------------------------------
+struct WtI32 {
+    typedef int32_t S;
+    typedef int32_t V;
+    static constexpr int LIMBS = 1;
+    static constexpr int CODE = 0;  // COUPE_INT
+    CG_HD static void limbs(S w, int, uint64_t *l) { l[0] = (uint32_t)w; }
+    CG_HD static V value(const uint64_t *l, int) { return (int32_t)(uint32_t)l[0]; }
+    CG_HD static V sub(V a, V b) { return (int32_t)((uint32_t)a - (uint32_t)b); }
+    CG_HD static bool less(V a, V b) { return a < b; }
+    CG_HD static double f64(V v) { return (double)v; }
+    CG_HD static uint64_t bits(V v) { return (uint64_t)(uint32_t)v; }
+    CG_HD static V from_bits(uint64_t b) { return (int32_t)(uint32_t)b; }
+};
+struct WtI64 {
+    typedef int64_t S;
+    typedef int64_t V;
+    static constexpr int LIMBS = 1;
+    static constexpr int CODE = 1;  // COUPE_INT64
+    CG_HD static void limbs(S w, int, uint64_t *l) { l[0] = (uint64_t)w; }
+    CG_HD static V value(const uint64_t *l, int) { return (int64_t)l[0]; }
+    CG_HD static V sub(V a, V b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+    CG_HD static bool less(V a, V b) { return a < b; }
+    CG_HD static double f64(V v) { return (double)v; }
+    CG_HD static uint64_t bits(V v) { return (uint64_t)v; }
+    CG_HD static V from_bits(uint64_t b) { return (int64_t)b; }
+};
+struct WtF64 {
+    typedef double S;
+    typedef double V;
+    static constexpr int LIMBS = 4;
+    static constexpr int CODE = 2;  // COUPE_DOUBLE
+    CG_HD static void limbs(S w, int s, uint64_t *l) {
+        unsigned __int128 q = fixed_q_bits(w, s);
+        l[0] = (uint32_t)q;
+        l[1] = (uint32_t)(q >> 32);
+        l[2] = (uint32_t)(q >> 64);
+        l[3] = (uint32_t)(q >> 96);
+    }
+    CG_HD static unsigned __int128 combine(const uint64_t *l) {
+        return (unsigned __int128)l[0] + ((unsigned __int128)l[1] << 32) + ((unsigned __int128)l[2] << 64) +
+               ((unsigned __int128)l[3] << 96);
+    }
+    CG_HD static V value(const uint64_t *l, int s) { return fixed_to_f64(combine(l), s); }
+    CG_HD static V sub(V a, V b) { return a - b; }
+    CG_HD static bool less(V a, V b) { return a < b; }
+    CG_HD static double f64(V v) { return v; }
+    CG_HD static uint64_t bits(V v) {
+#ifdef __CUDA_ARCH__
+        return (uint64_t)__double_as_longlong(v);
+#else
+        uint64_t b;
+        memcpy(&b, &v, 8);
+        return b;
+#endif
+    }
+    CG_HD static V from_bits(uint64_t b) {
+#ifdef __CUDA_ARCH__
+        return __longlong_as_double((long long)b);
+#else
+        double v;
+        memcpy(&v, &b, 8);
+        return v;
+#endif
+    }
+};
+
+// ---------------------------------------------------------------------------
+// One segment of a tree level (a contiguous range of the reordered arrays).
+// ---------------------------------------------------------------------------
+enum : uint32_t { SEG_ACTIVE = 0, SEG_DONE = 1, SEG_ALLLEFT = 2 };
+
+template <class KT>
+struct Seg {
+    typedef typename KT::T K;
+    uint64_t off;    // first item
+    uint64_t heap;   // heap id: children of h are 2h+1 and 2h+2 (wrapping)
+    uint64_t sum;    // weight sum (V bits)
+    uint64_t prev;   // prev_count_left of the split loop (UINT64_MAX first)
+    uint64_t wl;     // result: weight_left (V bits)
+    uint32_t n;      // items
+    uint32_t nleft;  // result: items sent left
+    uint32_t state;  // SEG_*
+    uint32_t steps;  // bisection steps taken so far
+    K lo, hi;        // current search interval on this level's axis
+    K pivot;         // result: items with key < pivot go left
+    K split_pos;     // result: the cut position
+    K bmin[3], bmax[3];
+};
+
+// Error bits raised by kernels (read by the host after each synchronisation).
+enum : uint32_t {
+    ERR_LOOKBACK_TIMEOUT = 1u,
+    ERR_SCATTER_BOUNDS = 2u,
+    ERR_NONFINITE_WEIGHT = 4u,
+    ERR_COUNT_MISMATCH = 8u,
+};
+
+// Device-side scalars of one run.
+struct RunScalars {
+    uint64_t bbox_min_ord[3];
+    uint64_t bbox_max_ord[3];
+    uint64_t wabs_max_bits;   // largest |w| as raw f64 bits (f64 weights)
+    uint64_t wsum_limbs[4];   // total weight
+    uint64_t nactive;         // segments still searching after a decide pass
+    uint64_t total_active;    // items in those segments
+    uint64_t nsegs_next;      // non-empty children of the level
+    uint64_t min_heap;        // smallest heap id of the last level
+    uint64_t ticket;          // dynamic chunk counter of the reorder
+    uint64_t steps_total;     // bisection steps summed over finished splits
+    uint64_t steps_max;
+    uint64_t splits;
+    uint32_t err;
+    int32_t fscale;
+};
+
+}  // namespace cg

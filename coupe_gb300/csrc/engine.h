@@ -1,0 +1,63 @@
+// Host-side interface between the C ABI (ffi.cpp) and the CUDA engine.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/coupe_gpu.h"
+
+namespace cg {
+
+// One Rcb run on device-resident data.
+struct RunArgs {
+    uint64_t n = 0;
+    int dim = 0;
+    const double *d_points = nullptr;  // n * dim doubles, AoS
+    int wtype = 0;                     // enum coupe_type
+    const void *d_weights = nullptr;   // n elements of wtype
+    uint64_t *d_part = nullptr;        // n part ids (output)
+    uint64_t iter_count = 0;
+    double tolerance = 0.0;
+    int mode = COUPE_GPU_REF32;
+    bool has_matrix = false;
+    double matrix[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // row-major dim x dim
+    cudaStream_t stream = nullptr;
+};
+
+// Per-device state: a stream, a grow-only workspace and pinned scalars.
+// Runs on one device are serialised by `mu`.
+struct DevCtx {
+    int dev = -1;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    void *ws = nullptr;
+    size_t ws_cap = 0;
+    void *h_pinned = nullptr;  // pinned host scratch for scalar read-backs
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;
+};
+
+// Returns the calling thread's current device context (created on first use).
+DevCtx *device_ctx(std::string *err);
+
+// Ensures the workspace holds at least `bytes`; returns a coupe_err.
+int ensure_workspace(DevCtx &C, size_t bytes, std::string *err);
+
+// Runs Rcb (the basis change of RunArgs applied first when has_matrix).
+int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
+
+// The Rib basis change (obb_to_aabb) of n device-resident points.
+int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
+               std::string *err);
+
+// Per-mode entry points, instantiated in separate translation units.
+int run_rcb_ref32(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
+int run_rcb_f64(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
+
+// Maps a CUDA error to a coupe_err and records a message.
+int cuda_fail(cudaError_t e, const char *what, std::string *err);
+
+}  // namespace cg

@@ -1,0 +1,266 @@
+// Device contexts, workspace management, mode dispatch and the Rib basis
+// change (OrientedBoundingBox::from_points, coupe/src/geometry.rs:210-228).
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+
+#include "engine.h"
+#include "kernels.cuh"
+
+namespace cg {
+
+int cuda_fail(cudaError_t e, const char *what, std::string *err) {
+    if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+    cudaGetLastError();  // clear a sticky launch error of this thread
+    return e == cudaErrorMemoryAllocation ? COUPE_ERR_ALLOC : COUPE_ERR_CRASH;
+}
+
+static std::mutex g_ctx_mu;
+static std::map<int, std::unique_ptr<DevCtx>> g_ctx;
+
+DevCtx *device_ctx(std::string *err) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        cuda_fail(e, "cudaGetDevice", err);
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> g(g_ctx_mu);
+    auto it = g_ctx.find(dev);
+    if (it != g_ctx.end()) return it->second.get();
+    std::unique_ptr<DevCtx> c(new DevCtx());
+    c->dev = dev;
+    if ((e = cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaMallocHost(&c->h_pinned, 4096)) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
+        cuda_fail(e, "device context", err);
+        return nullptr;
+    }
+    DevCtx *r = c.get();
+    g_ctx[dev] = std::move(c);
+    return r;
+}
+
+int ensure_workspace(DevCtx &C, size_t bytes, std::string *err) {
+    if (bytes <= C.ws_cap) return COUPE_ERR_OK;
+    if (C.ws) {
+        cudaStreamSynchronize(C.stream);
+        cudaFree(C.ws);
+        C.ws = nullptr;
+        C.ws_cap = 0;
+    }
+    size_t cap = bytes + bytes / 8;
+    cudaError_t e = cudaMalloc(&C.ws, cap);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc workspace", err);
+    C.ws_cap = cap;
+    return COUPE_ERR_OK;
+}
+
+int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
+    st->mode = a.mode;
+    switch (a.mode) {
+    case COUPE_GPU_REF32:
+        return run_rcb_ref32(C, a, st, err);
+    case COUPE_GPU_F64:
+        return run_rcb_f64(C, a, st, err);
+    default:
+        if (err) *err = "precision mode not available in this build";
+        return COUPE_ERR_BAD_TYPE;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Rib basis change.  inertia_matrix (geometry.rs:273-284) is unweighted: the
+// centroid sum(p)/n, then sum((p-c)(p-c)^T).  Both sums are reduced in a fixed
+// order (fixed grid, fixed tree inside each block, blocks summed in index
+// order on the host), so the result does not change from run to run.
+// ---------------------------------------------------------------------------
+constexpr int RIB_GRID = 1024;
+
+template <int D>
+__global__ void __launch_bounds__(BLOCK) k_moments(const double *__restrict__ pts, uint64_t n, const double *center,
+                                                   double *partial) {
+    __shared__ double sh[D * D][NWARPS];
+    double acc[D * D];
+#pragma unroll
+    for (int k = 0; k < D * D; ++k) acc[k] = 0.0;
+    double c[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) c[d] = center ? center[d] : 0.0;
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        double o[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) o[d] = __dsub_rn(pts[i * D + d], c[d]);
+        if (!center) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) acc[d] = __dadd_rn(acc[d], o[d]);
+        } else {
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b = 0; b < D; ++b) acc[a * D + b] = __dadd_rn(acc[a * D + b], __dmul_rn(o[a], o[b]));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int K = center ? D * D : D;
+    for (int k = 0; k < K; ++k) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+        if (lane == 0) sh[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double v = 0.0;
+        for (int w = 0; w < NWARPS; ++w) v = __dadd_rn(v, sh[threadIdx.x][w]);
+        partial[blockIdx.x * D * D + threadIdx.x] = v;
+    }
+}
+
+// Symmetric eigenvectors by cyclic Jacobi rotations (Golub & Van Loan,
+// Matrix Computations, section 8.5), columns of v.
+static void sym_eigen(const double *a_in, int n, double *ev, double *v) {
+    double a[9];
+    std::memcpy(a, a_in, sizeof(double) * n * n);
+    for (int i = 0; i < n * n; ++i) v[i] = 0.0;
+    for (int i = 0; i < n; ++i) v[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int p = 0; p < n; ++p) {
+            diag += a[p * n + p] * a[p * n + p];
+            for (int q = p + 1; q < n; ++q) off += a[p * n + q] * a[p * n + q];
+        }
+        if (off == 0.0 || off <= 1e-300 * diag) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = a[p * n + q];
+                if (apq == 0.0) continue;
+                const double tau = (a[q * n + q] - a[p * n + p]) / (2.0 * apq);
+                const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+                for (int k = 0; k < n; ++k) {  // A <- A J
+                    const double x = a[k * n + p], y = a[k * n + q];
+                    a[k * n + p] = c * x - s * y;
+                    a[k * n + q] = s * x + c * y;
+                }
+                for (int k = 0; k < n; ++k) {  // A <- J^T A
+                    const double x = a[p * n + k], y = a[q * n + k];
+                    a[p * n + k] = c * x - s * y;
+                    a[q * n + k] = s * x + c * y;
+                }
+                for (int k = 0; k < n; ++k) {  // V <- V J
+                    const double x = v[k * n + p], y = v[k * n + q];
+                    v[k * n + p] = c * x - s * y;
+                    v[k * n + q] = s * x + c * y;
+                }
+            }
+    }
+    for (int i = 0; i < n; ++i) ev[i] = a[i * n + i];
+}
+
+// approx 0.5's default ulps comparison: |a-b| <= f64::EPSILON, else same sign
+// and at most 4 representable values apart.
+static bool ulps_close(double a, double b) {
+    if (std::fabs(a - b) <= 2.220446049250313e-16) return true;
+    if (std::signbit(a) != std::signbit(b)) return false;
+    int64_t x, y;
+    std::memcpy(&x, &a, 8);
+    std::memcpy(&y, &b, 8);
+    return (x > y ? x - y : y - x) <= 4;
+}
+
+// householder_reflection (geometry.rs:305-319) then its inverse (:219).
+static bool obb_matrix(const double *inertia, int D, double *out) {
+    double ev[3], V[9], v[3];
+    sym_eigen(inertia, D, ev, V);
+    int best = 0;
+    for (int i = 1; i < D; ++i)
+        if (ev[i] > ev[best]) best = i;
+    for (int i = 0; i < D; ++i) v[i] = V[i * D + best];
+    double nn = 0.0;
+    for (int i = 0; i < D; ++i) nn += v[i] * v[i];
+    const double nrm = std::sqrt(nn);
+    double H[9];
+    for (int i = 0; i < D * D; ++i) H[i] = 0.0;
+    for (int i = 0; i < D; ++i) H[i * D + i] = 1.0;
+    bool parallel = true;
+    for (int i = 0; i < D; ++i) parallel = parallel && ulps_close(v[i] / nrm, i == 0 ? 1.0 : 0.0);
+    if (!parallel) {
+        const double sign = v[0] > 0.0 ? -1.0 : 1.0;
+        double w[3];
+        for (int i = 0; i < D; ++i) w[i] = v[i] + (i == 0 ? sign * nrm : 0.0);
+        double wtw = 0.0;
+        for (int i = 0; i < D; ++i) wtw += w[i] * w[i];
+        for (int i = 0; i < D; ++i)
+            for (int j = 0; j < D; ++j) H[i * D + j] -= 2.0 * w[i] * w[j] / wtw;
+    }
+    // inverse by the adjugate
+    if (D == 2) {
+        const double det = H[0] * H[3] - H[1] * H[2];
+        if (det == 0.0) return false;
+        out[0] = H[3] / det;
+        out[1] = -H[1] / det;
+        out[2] = -H[2] / det;
+        out[3] = H[0] / det;
+        return true;
+    }
+    double cof[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int r0 = (i + 1) % 3, r1 = (i + 2) % 3, c0 = (j + 1) % 3, c1 = (j + 2) % 3;
+            cof[i * 3 + j] = H[r0 * 3 + c0] * H[r1 * 3 + c1] - H[r0 * 3 + c1] * H[r1 * 3 + c0];
+        }
+    const double det = H[0] * cof[0] + H[1] * cof[1] + H[2] * cof[2];
+    if (det == 0.0) return false;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) out[i * 3 + j] = cof[j * 3 + i] / det;
+    return true;
+}
+
+int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
+               std::string *err) {
+    cudaStream_t s = stream ? stream : C.stream;
+    const size_t part_bytes = (size_t)RIB_GRID * 9 * sizeof(double);
+    int rc = ensure_workspace(C, part_bytes + 4 * sizeof(double), err);
+    if (rc != COUPE_ERR_OK) return rc;
+    double *d_part = (double *)C.ws;
+    double *d_c = d_part + RIB_GRID * 9;  // the centroid, after the partials
+    std::unique_ptr<double[]> h(new double[RIB_GRID * 9]);
+    double center[3] = {0, 0, 0};
+    // pass 1: centroid
+    cudaError_t e;
+    if (dim == 2)
+        k_moments<2><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, nullptr, d_part);
+    else
+        k_moments<3><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, nullptr, d_part);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_moments", err);
+    if ((e = cudaMemcpyAsync(h.get(), d_part, part_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "centroid", err);
+    for (int b = 0; b < RIB_GRID; ++b)
+        for (int d = 0; d < dim; ++d) center[d] += h[b * dim * dim + d];
+    for (int d = 0; d < dim; ++d) center[d] = center[d] / (double)n;
+    // pass 2: second moments about the centroid
+    if ((e = cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "centroid upload", err);
+    if (dim == 2)
+        k_moments<2><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_c, d_part);
+    else
+        k_moments<3><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_c, d_part);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_moments", err);
+    if ((e = cudaMemcpyAsync(h.get(), d_part, part_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "inertia", err);
+    double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < RIB_GRID; ++b)
+        for (int k = 0; k < dim * dim; ++k) m[k] += h[b * dim * dim + k];
+    if (!obb_matrix(m, dim, out)) {
+        if (err) *err = "singular basis change";
+        return COUPE_ERR_CRASH;
+    }
+    return COUPE_ERR_OK;
+}
+
+}  // namespace cg

@@ -1,0 +1,358 @@
+// The C ABI of libcoupe_gpu.so (include/coupe.h, include/coupe_gpu.h).
+//
+// Semantics follow coupe-ffi (coupe-ffi/src/lib.rs, coupe-ffi/src/data.rs):
+// data sets are arrays, constants or callbacks; points are always read as
+// `dimension` doubles per item whatever the data set's type; the length
+// mismatch is reported before a bad dimension; an empty input succeeds and
+// leaves `partition` untouched.  Host inputs are gathered into pinned staging
+// memory, copied to the device, partitioned there, and the ids copied back.
+#include <cuda_runtime.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/coupe.h"
+#include "../../include/coupe_gpu.h"
+#include "engine.h"
+
+struct coupe_data {
+    int kind;  // 0 array, 1 constant, 2 callback
+    uintptr_t len;
+    int type;
+    const void *ptr;  // array base or constant value
+    const void *ctx;
+    const void *(*i_th)(const void *, uintptr_t);
+};
+
+namespace {
+
+thread_local std::string t_err;
+thread_local coupe_gpu_stats t_stats;
+
+size_t type_size(int t) { return t == COUPE_INT ? 4 : 8; }
+
+coupe_data *new_data(int kind, uintptr_t len, int type, const void *ptr, const void *ctx,
+                     const void *(*f)(const void *, uintptr_t)) {
+    coupe_data *d = new (std::nothrow) coupe_data;
+    if (!d) return nullptr;
+    d->kind = kind;
+    d->len = len;
+    d->type = type;
+    d->ptr = ptr;
+    d->ctx = ctx;
+    d->i_th = f;
+    return d;
+}
+
+// Copies element i (elem bytes) of a data set to dst.
+inline void fetch(const coupe_data *d, uintptr_t i, size_t elem, void *dst) {
+    switch (d->kind) {
+    case 0:
+        std::memcpy(dst, (const char *)d->ptr + i * elem, elem);
+        break;
+    case 1:
+        std::memcpy(dst, d->ptr, elem);
+        break;
+    default:
+        std::memcpy(dst, d->i_th(d->ctx, i), elem);
+        break;
+    }
+}
+
+// Pinned staging buffers reused across calls on this thread.
+struct Staging {
+    void *p = nullptr;
+    size_t cap = 0;
+    ~Staging() {
+        if (p) cudaFreeHost(p);
+    }
+    void *get(size_t bytes) {
+        if (bytes <= cap) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cap = bytes;
+        return p;
+    }
+};
+
+// Device buffers for host calls, reused across calls on this thread.
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int dev = -1;
+    void *get(size_t bytes, int device) {
+        if (bytes <= cap && device == dev) return p;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMalloc(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        cap = bytes;
+        dev = device;
+        return p;
+    }
+};
+
+thread_local DevBuf t_dev;
+
+// Is [p, p+bytes) pinned (page-locked or registered) host memory?
+bool is_pinned(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// Host-side call: validate like coupe-ffi, stage, run on the device, copy back.
+coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                    const coupe_data *weights, uintptr_t iter_count, double tolerance, int mode) {
+    t_err.clear();
+    std::memset(&t_stats, 0, sizeof(t_stats));
+    t_stats.mode = mode;
+    if (!points || !weights) {
+        t_err = "NULL data set";
+        return COUPE_ERR_CRASH;
+    }
+    const uintptr_t n = points->len;
+    if (n != weights->len) return COUPE_ERR_LEN_MISMATCH;  // coupe-ffi/src/lib.rs:285-288
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;  // :297-301
+    if (weights->type < COUPE_INT || weights->type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (n == 0) return COUPE_ERR_OK;  // recursive_bisection.rs:685-688
+    if (!partition) {
+        t_err = "NULL partition";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    const size_t pbytes = (size_t)n * dimension * sizeof(double);
+    const size_t wsz = type_size(weights->type);
+    const size_t wbytes = (size_t)n * wsz;
+    const size_t obytes = (size_t)n * sizeof(uint64_t);
+    std::lock_guard<std::mutex> lock(C->mu);
+    cudaStream_t s = C->stream;
+    char *dbuf = (char *)t_dev.get(pbytes + wbytes + obytes + 512, C->dev);
+    if (!dbuf) {
+        t_err = "device allocation of the input copy failed";
+        return COUPE_ERR_ALLOC;
+    }
+    double *d_pts = (double *)dbuf;
+    char *d_w = dbuf + ((pbytes + 255) & ~(size_t)255);
+    uint64_t *d_part = (uint64_t *)(d_w + ((wbytes + 255) & ~(size_t)255));
+    cudaError_t e;
+    // points: arrays are copied as they are; constants and callbacks are
+    // gathered into pinned staging first (coupe-ffi/src/data.rs:156-165).
+    static thread_local Staging st_p, st_w;
+    const void *src_p = points->ptr;
+    if (points->kind != 0) {
+        double *h = (double *)st_p.get(pbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(points, i, dimension * sizeof(double), h + i * dimension);
+        src_p = h;
+    }
+    const void *src_w = weights->ptr;
+    if (weights->kind != 0) {
+        char *h = (char *)st_w.get(wbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(weights, i, wsz, h + i * wsz);
+        src_w = h;
+    }
+    if ((e = cudaMemcpyAsync(d_pts, src_p, pbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+        int rc = cg::cuda_fail(e, "host to device copy", &t_err);
+        return (coupe_err)rc;
+    }
+    cg::RunArgs a;
+    a.n = n;
+    a.dim = (int)dimension;
+    a.d_points = d_pts;
+    a.wtype = weights->type;
+    a.d_weights = d_w;
+    a.d_part = d_part;
+    a.iter_count = iter_count;
+    a.tolerance = tolerance;
+    a.mode = mode;
+    a.stream = s;
+    int rc = COUPE_ERR_OK;
+    if (rib) {
+        double M[9];
+        rc = cg::rib_matrix(*C, n, (int)dimension, d_pts, s, M, &err);
+        if (rc == COUPE_ERR_OK) {
+            a.has_matrix = true;
+            std::memcpy(a.matrix, M, sizeof(M));
+        }
+    }
+    if (rc == COUPE_ERR_OK) rc = cg::run_rcb(*C, a, &t_stats, &err);
+    if (rc != COUPE_ERR_OK) {
+        t_err = err;
+        return (coupe_err)rc;
+    }
+    static_assert(sizeof(uintptr_t) == sizeof(uint64_t), "64-bit uintptr_t expected");
+    if ((e = cudaMemcpyAsync(partition, d_part, obytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "device to host copy", &t_err);
+    return COUPE_ERR_OK;
+}
+
+coupe_err device_call(bool rib, uint64_t *d_partition, uint64_t n, uint64_t dimension, const double *d_points,
+                      coupe_type wtype, const void *d_weights, uint64_t iter_count, double tolerance, int mode,
+                      const double *matrix, void *stream) {
+    t_err.clear();
+    std::memset(&t_stats, 0, sizeof(t_stats));
+    t_stats.mode = mode;
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (wtype < COUPE_INT || wtype > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (n == 0) return COUPE_ERR_OK;
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    cg::RunArgs a;
+    a.n = n;
+    a.dim = (int)dimension;
+    a.d_points = d_points;
+    a.wtype = wtype;
+    a.d_weights = d_weights;
+    a.d_part = d_partition;
+    a.iter_count = iter_count;
+    a.tolerance = tolerance;
+    a.mode = mode;
+    a.stream = (cudaStream_t)stream;
+    int rc = COUPE_ERR_OK;
+    if (rib) {
+        double M[9];
+        rc = cg::rib_matrix(*C, n, (int)dimension, d_points, a.stream, M, &err);
+        if (rc == COUPE_ERR_OK) {
+            a.has_matrix = true;
+            std::memcpy(a.matrix, M, sizeof(M));
+        }
+    } else if (matrix) {
+        a.has_matrix = true;
+        std::memcpy(a.matrix, matrix, sizeof(double) * dimension * dimension);
+    }
+    if (rc == COUPE_ERR_OK) rc = cg::run_rcb(*C, a, &t_stats, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *coupe_strerror(enum coupe_err err) {
+    switch (err) {
+    case COUPE_ERR_OK: return "success";
+    case COUPE_ERR_ALLOC: return "allocation failed";
+    case COUPE_ERR_CRASH: return "coupe encountered a bug and crashed";
+    case COUPE_ERR_BAD_DIMENSION: return "this algorithm does not support the given mesh dimension";
+    case COUPE_ERR_BAD_TYPE: return "this algorithm does not support the given type";
+    case COUPE_ERR_BIPART_ONLY: return "this algorithm does not support k-way partitioning";
+    case COUPE_ERR_LEN_MISMATCH: return "input iters (e.g. weights and points) don't have the same length";
+    case COUPE_ERR_NOT_FOUND: return "no partition has been found for the given constraints";
+    case COUPE_ERR_NEG_VALUES: return "this algorithm does not support negative values";
+    }
+    return "unknown error";
+}
+
+void coupe_data_free(coupe_data *data) { delete data; }
+
+coupe_data *coupe_data_array(uintptr_t len, enum coupe_type type, const void *data) {
+    return new_data(0, len, type, data, nullptr, nullptr);
+}
+
+coupe_data *coupe_data_constant(uintptr_t len, enum coupe_type type, const void *value) {
+    return new_data(1, len, type, value, nullptr, nullptr);
+}
+
+coupe_data *coupe_data_fn(const void *context, uintptr_t len, enum coupe_type type,
+                          const void *(*i_th)(const void *, uintptr_t)) {
+    return new_data(2, len, type, nullptr, context, i_th);
+}
+
+enum coupe_err coupe_rcb(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                         const coupe_data *weights, uintptr_t iter_count, double tolerance) {
+    return host_call(false, partition, dimension, points, weights, iter_count, tolerance, COUPE_GPU_REF32);
+}
+
+enum coupe_err coupe_rib(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                         const coupe_data *weights, uintptr_t iter_count, double tolerance) {
+    return host_call(true, partition, dimension, points, weights, iter_count, tolerance, COUPE_GPU_REF32);
+}
+
+enum coupe_err coupe_gpu_rcb(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                             const coupe_data *weights, uintptr_t iter_count, double tolerance, int mode) {
+    return host_call(false, partition, dimension, points, weights, iter_count, tolerance, mode);
+}
+
+enum coupe_err coupe_gpu_rib(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                             const coupe_data *weights, uintptr_t iter_count, double tolerance, int mode) {
+    return host_call(true, partition, dimension, points, weights, iter_count, tolerance, mode);
+}
+
+enum coupe_err coupe_gpu_rcb_device(uint64_t *d_partition, uint64_t n, uint64_t dimension, const double *d_points,
+                                    enum coupe_type weight_type, const void *d_weights, uint64_t iter_count,
+                                    double tolerance, int mode, const double *matrix, void *stream) {
+    return device_call(false, d_partition, n, dimension, d_points, weight_type, d_weights, iter_count, tolerance, mode,
+                       matrix, stream);
+}
+
+enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t dimension, const double *d_points,
+                                    enum coupe_type weight_type, const void *d_weights, uint64_t iter_count,
+                                    double tolerance, int mode, void *stream) {
+    return device_call(true, d_partition, n, dimension, d_points, weight_type, d_weights, iter_count, tolerance, mode,
+                       nullptr, stream);
+}
+
+enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double *d_points, double *obb_to_aabb,
+                                    void *stream) {
+    t_err.clear();
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (n == 0) {
+        t_err = "no points";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    int rc = cg::rib_matrix(*C, n, (int)dimension, d_points, (cudaStream_t)stream, obb_to_aabb, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+void coupe_gpu_last_stats(struct coupe_gpu_stats *out) {
+    if (out) *out = t_stats;
+}
+
+const char *coupe_gpu_last_error(void) { return t_err.c_str(); }
+
+const char *coupe_gpu_version(void) { return "coupe-gpu 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,888 @@
+// CUDA kernels of the GB300 Rcb/Rib engine (sm_103a).
+//
+// A tree level is a list of segments (contiguous ranges of the reordered
+// point arrays).  Per level:
+//   k_hist    streams the keys and weights of the segments still searching
+//             and bins them, per segment, on the 2^nbk - 1 candidate cuts
+//             that the next nbk bisection steps of coupe's split loop can
+//             visit (recursive_bisection.rs:471-572): count, weight and
+//             smallest key per bin.
+//   k_decide  replays up to nbk steps of that loop exactly from the bins
+//             (one warp per segment) and either finishes the split or sets
+//             up the next interval.
+//   k_reorder once every split of the level is final, moves each segment's
+//             items into [left | right] children (stable), replacing
+//             reorder_split (recursive_bisection.rs:122-181, 437-453).
+//   k_assign  on the last level writes the part ids directly.
+// All device-side waits are bounded and report through RunScalars::err.
+#pragma once
+
+#include "common.cuh"
+
+namespace cg {
+
+constexpr int BLOCK = 256;
+constexpr int NWARPS = BLOCK / 32;
+constexpr int MAX_NBK = 8;
+constexpr int MAX_NB = 1 << MAX_NBK;
+constexpr int HIST_ITEMS = 16;               // items per thread per hist iteration
+constexpr int R_ITEMS = 8;                   // items per thread per reorder tile
+constexpr int R_TILE = BLOCK * R_ITEMS;      // 2048
+constexpr uint64_t LB_AGG = 1ull << 62;      // look-back: aggregate published
+constexpr uint64_t LB_INCL = 2ull << 62;     // look-back: inclusive prefix published
+constexpr uint64_t LB_VALUE = (1ull << 62) - 1;
+constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
+
+// ---------------------------------------------------------------------------
+// Small reductions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ uint32_t warp_min_u32(uint32_t v) { return __reduce_min_sync(0xffffffffu, v); }
+
+template <class O>
+__device__ __forceinline__ O warp_min_ord(O v);
+template <>
+__device__ __forceinline__ uint32_t warp_min_ord<uint32_t>(uint32_t v) {
+    return warp_min_u32(v);
+}
+template <>
+__device__ __forceinline__ uint64_t warp_min_ord<uint64_t>(uint64_t v) {
+    return warp_min_u64(v);
+}
+
+// Exclusive scan of one u64 per thread over the block; returns the prefix
+// and writes the block total.  `sh` holds NWARPS + 1 words.
+__device__ __forceinline__ uint64_t block_exscan_u64(uint64_t v, uint64_t *sh, uint64_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) sh[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0;
+        uint64_t ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t u = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += u;
+        }
+        if (lane < (int)(blockDim.x >> 5)) sh[lane] = ti - t;
+        if (lane == 31) sh[32] = ti;
+    }
+    __syncthreads();
+    uint64_t r = sh[warp] + inc - v;
+    total = sh[32];
+    __syncthreads();
+    return r;
+}
+
+// Largest k with P[k] <= x, for P non-decreasing of length len (P[0] <= x).
+__device__ __forceinline__ uint32_t upper_index(const uint64_t *P, uint32_t len, uint64_t x) {
+    uint32_t lo = 0, hi = len;  // invariant: P[lo] <= x, answer in [lo, hi)
+    while (hi - lo > 1) {
+        uint32_t m = (lo + hi) >> 1;
+        if (P[m] <= x)
+            lo = m;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
+template <class KT>
+__device__ __forceinline__ uint32_t seg_index_of(const Seg<KT> *segs, uint32_t S, uint64_t x) {
+    uint32_t lo = 0, hi = S;
+    while (hi - lo > 1) {
+        uint32_t m = (lo + hi) >> 1;
+        if (segs[m].off <= x)
+            lo = m;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void atomic_max_ord(uint32_t *p, uint32_t v) { atomicMax(p, v); }
+__device__ __forceinline__ void atomic_max_ord(uint64_t *p, uint64_t v) {
+    atomicMax((unsigned long long *)p, (unsigned long long)v);
+}
+
+struct Mat {
+    double m[9];
+    int on;
+};
+
+// ---------------------------------------------------------------------------
+// k_convert: AoS f64 points -> D SoA key arrays (coupe's `point[coord] as
+// f32`, recursive_bisection.rs:674-679), optionally after the Rib basis change
+// p' = M p accumulated column by column (geometry.rs:203-205), and the f64
+// bounding box (BoundingBox::from_points, geometry.rs:33-78: NaN never
+// updates, the fold starts at f64::MAX / f64::MIN).
+// ---------------------------------------------------------------------------
+template <int D, class KT>
+__global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pts, uint64_t n, Mat M,
+                                                   typename KT::T *__restrict__ k0,
+                                                   typename KT::T *__restrict__ k1,
+                                                   typename KT::T *__restrict__ k2, RunScalars *rs) {
+    typedef typename KT::T K;
+    uint64_t mn[3], mx[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = ord_f64(1.7976931348623157e308);
+        mx[d] = ord_f64(-1.7976931348623157e308);
+    }
+    K *outs[3] = {k0, k1, k2};
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        double p[D], q[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) p[d] = pts[i * D + d];
+        if (M.on) {
+#pragma unroll
+            for (int r = 0; r < D; ++r) {
+                double acc = __dmul_rn(M.m[r * D + 0], p[0]);
+#pragma unroll
+                for (int c = 1; c < D; ++c) acc = __dadd_rn(acc, __dmul_rn(M.m[r * D + c], p[c]));
+                q[r] = acc;
+            }
+        } else {
+#pragma unroll
+            for (int d = 0; d < D; ++d) q[d] = p[d];
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            outs[d][i] = KT::from_f64(q[d]);
+            if (q[d] == q[d]) {
+                uint64_t o = ord_f64(q[d]);
+                mn[d] = o < mn[d] ? o : mn[d];
+                mx[d] = o > mx[d] ? o : mx[d];
+            }
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        uint64_t a = warp_min_u64(mn[d]);
+        uint64_t b = warp_max_u64(mx[d]);
+        if ((threadIdx.x & 31) == 0) {
+            atomicMin((unsigned long long *)&rs->bbox_min_ord[d], (unsigned long long)a);
+            atomicMax((unsigned long long *)&rs->bbox_max_ord[d], (unsigned long long)b);
+        }
+    }
+}
+
+// Largest |w| of f64 weights as raw bits (non-finite values sort above).
+static __global__ void __launch_bounds__(BLOCK) k_wabs_max(const double *__restrict__ w, uint64_t n, RunScalars *rs) {
+    uint64_t m = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        uint64_t b = (uint64_t)__double_as_longlong(w[i]) & 0x7fffffffffffffffull;
+        m = b > m ? b : m;
+    }
+    m = warp_max_u64(m);
+    if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&rs->wabs_max_bits, (unsigned long long)m);
+}
+
+__device__ __forceinline__ int run_fscale(const RunScalars *rs, uint64_t n) {
+    return fixed_scale_from_max(__longlong_as_double((long long)rs->wabs_max_bits), n);
+}
+
+// Total weight (recursive_bisection.rs:684), order independent.
+template <class WT>
+__global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict__ w, uint64_t n, RunScalars *rs) {
+    const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
+    uint64_t acc[WT::LIMBS];
+#pragma unroll
+    for (int l = 0; l < WT::LIMBS; ++l) acc[l] = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        uint64_t q[WT::LIMBS];
+        WT::limbs(w[i], fs, q);
+#pragma unroll
+        for (int l = 0; l < WT::LIMBS; ++l) acc[l] += q[l];
+    }
+#pragma unroll
+    for (int l = 0; l < WT::LIMBS; ++l) {
+        uint64_t v = warp_sum_u64(acc[l]);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long *)&rs->wsum_limbs[l], (unsigned long long)v);
+    }
+}
+
+// Root segment of level 0 (rcb_recurse's first call, recursive_bisection.rs:696).
+template <class KT, class WT>
+__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs) {
+    typedef typename KT::T K;
+    const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
+    rs->fscale = fs;
+    if (WT::LIMBS > 1 && rs->wabs_max_bits >= 0x7ff0000000000000ull) rs->err |= ERR_NONFINITE_WEIGHT;
+    Seg<KT> s;
+    s.off = 0;
+    s.heap = 0;
+    s.sum = WT::bits(WT::value(rs->wsum_limbs, fs));
+    s.prev = ~0ull;
+    s.wl = 0;
+    s.n = (uint32_t)n;
+    s.nleft = 0;
+    s.state = SEG_ACTIVE;
+    s.steps = 0;
+    for (int d = 0; d < 3; ++d) {
+        double a = d < D ? unord_f64(rs->bbox_min_ord[d]) : 0.0;
+        double b = d < D ? unord_f64(rs->bbox_max_ord[d]) : 0.0;
+        s.bmin[d] = KT::from_f64(a);
+        s.bmax[d] = KT::from_f64(b);
+    }
+    s.lo = s.bmin[0];
+    s.hi = s.bmax[0];
+    s.pivot = 0;
+    s.split_pos = 0;
+    segs[0] = s;
+    list[0] = 0;
+    P[0] = 0;
+    P[1] = n;
+}
+
+// ---------------------------------------------------------------------------
+// Candidate-cut tree of a segment: node i (heap order) holds the cut that
+// coupe's loop computes after the decisions spelled by i's path from the
+// root; leaves (bins) are in key order.
+// ---------------------------------------------------------------------------
+template <class KT>
+__device__ __forceinline__ void build_cuts(typename KT::T lo, typename KT::T hi, int nbk, typename KT::T *cuts) {
+    typedef typename KT::T K;
+    const int nodes = (1 << nbk) - 1;
+    for (int i = threadIdx.x; i < nodes; i += blockDim.x) {
+        const uint32_t id1 = (uint32_t)i + 1;  // 1-based heap id
+        const int depth = 31 - __clz(id1);
+        K a = lo, b = hi;
+        for (int l = depth - 1; l >= 0; --l) {
+            K c = KT::mid(a, b);
+            if ((id1 >> l) & 1)
+                a = c;
+            else
+                b = c;
+        }
+        cuts[i] = KT::mid(a, b);
+    }
+}
+
+template <class KT>
+__device__ __forceinline__ int bin_of(typename KT::T key, const typename KT::T *cuts, int nbk) {
+    int node = 0;
+    for (int l = 0; l < nbk; ++l) node = 2 * node + 1 + (key < cuts[node] ? 0 : 1);
+    return node - ((1 << nbk) - 1);
+}
+
+// Global histogram slots: [segment][bin]; bmin stores ~ord(key) so that an
+// all-zero slot means "no key" and atomicMax of ~ord is a min of keys.
+template <class KT, class WT>
+struct Hist {
+    uint32_t *cnt;
+    uint64_t *w;  // [seg][bin][LIMBS]
+    typename KT::Ord *inv;
+};
+
+// ---------------------------------------------------------------------------
+// k_hist: one static chunk of the active items per CTA.
+// ---------------------------------------------------------------------------
+template <class KT, class WT>
+__global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+                                                const uint64_t *__restrict__ P, uint32_t nlist,
+                                                const typename KT::T *__restrict__ keys,
+                                                const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
+                                                uint64_t n_total, const RunScalars *rs) {
+    typedef typename KT::T K;
+    typedef typename KT::Ord O;
+    constexpr int L = WT::LIMBS;
+    __shared__ K cuts[MAX_NB];
+    __shared__ uint32_t scnt[MAX_NB];
+    __shared__ uint64_t sw[MAX_NB * L];
+    __shared__ O sinv[MAX_NB];
+    const int NB = 1 << nbk;
+    const int fs = L > 1 ? rs->fscale : 0;
+    const uint64_t T = P[nlist];
+    const uint64_t c0 = T * blockIdx.x / gridDim.x, c1 = T * (blockIdx.x + 1) / gridDim.x;
+    if (c0 >= c1) return;
+    uint32_t k = upper_index(P, nlist + 1, c0);
+    uint64_t pos = c0;
+    while (pos < c1) {
+        const uint32_t s = list[k];
+        const uint64_t pe = min(c1, P[k + 1]);
+        const Seg<KT> &sg = segs[s];
+        const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
+        const K lo = sg.lo, hi = sg.hi;
+        __syncthreads();
+        build_cuts<KT>(lo, hi, nbk, cuts);
+        for (int i = threadIdx.x; i < NB; i += BLOCK) {
+            scnt[i] = 0;
+            sinv[i] = 0;
+#pragma unroll
+            for (int l = 0; l < L; ++l) sw[i * L + l] = 0;
+        }
+        __syncthreads();
+        for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HIST_ITEMS) {
+            K kv[HIST_ITEMS];
+            typename WT::S wv[HIST_ITEMS];
+#pragma unroll
+            for (int i = 0; i < HIST_ITEMS; ++i) {
+                const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                if (e < b) {
+                    kv[i] = keys[e];
+                    wv[i] = wts[e];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < HIST_ITEMS; ++i) {
+                const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                if (e < b && kv[i] == kv[i]) {
+                    const int bin = bin_of<KT>(kv[i], cuts, nbk);
+                    atomicAdd(&scnt[bin], 1u);
+                    uint64_t q[L];
+                    WT::limbs(wv[i], fs, q);
+#pragma unroll
+                    for (int l = 0; l < L; ++l)
+                        if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
+                    atomic_max_ord(&sinv[bin], (O)~KT::ord(kv[i]));
+                }
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < NB; i += BLOCK) {
+            if (scnt[i]) {
+                const size_t g = (size_t)s * NB + i;
+                atomicAdd(&H.cnt[g], scnt[i]);
+#pragma unroll
+                for (int l = 0; l < L; ++l)
+                    if (sw[i * L + l]) atomicAdd((unsigned long long *)&H.w[g * L + l], (unsigned long long)sw[i * L + l]);
+                atomic_max_ord(&H.inv[g], sinv[i]);
+            }
+        }
+        pos = pe;
+        ++k;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_decide: replays coupe's split loop (recursive_bisection.rs:470-572) for
+// up to nbk steps per segment from its bins.  One warp per listed segment;
+// every lane computes the same decisions.
+// ---------------------------------------------------------------------------
+template <class KT, class WT>
+__global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
+                                                  Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
+                                                  RunScalars *rs) {
+    typedef typename KT::T K;
+    typedef typename KT::Ord O;
+    typedef typename WT::V V;
+    constexpr int L = WT::LIMBS;
+    const int lane = threadIdx.x & 31;
+    const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
+    if (k >= nlist) return;
+    const uint32_t s = list[k];
+    Seg<KT> sg = segs[s];
+    const int NB = 1 << nbk;
+    const int per = NB >= 32 ? NB / 32 : 1;
+    const int fs = L > 1 ? rs->fscale : 0;
+    // owned bins: [lane*per, lane*per + per)
+    uint32_t bc[MAX_NB / 32];
+    uint64_t bw[MAX_NB / 32][L];
+    O bm[MAX_NB / 32];
+#pragma unroll
+    for (int j = 0; j < MAX_NB / 32; ++j) {
+        const int b = lane * per + j;
+        const bool own = j < per && b < NB;
+        const size_t g = (size_t)s * NB + b;
+        bc[j] = own ? H.cnt[g] : 0;
+#pragma unroll
+        for (int l = 0; l < L; ++l) bw[j][l] = own ? H.w[g * L + l] : 0;
+        O inv = own ? H.inv[g] : (O)0;
+        O o = (O)~inv;
+        bm[j] = o > KT::ORD_INF ? KT::ORD_INF : o;
+    }
+    const V sum = WT::from_bits(sg.sum);
+    K lo = sg.lo, hi = sg.hi;
+    uint64_t prev = sg.prev;
+    int lo_b = 0, hi_b = NB;
+    uint64_t cnt_below = 0;
+    uint64_t w_below[L];
+#pragma unroll
+    for (int l = 0; l < L; ++l) w_below[l] = 0;
+    O kmin_above = KT::ORD_INF;
+    uint32_t state = SEG_ACTIVE;
+    uint32_t steps = 0;
+    K pivot = 0, split_pos = 0;
+    V wl_out = 0;
+    uint64_t nleft = 0;
+    for (int step = 0; step < nbk; ++step) {
+        const int mid_b = (lo_b + hi_b) >> 1;
+        uint64_t c = 0;
+        uint64_t wp[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) wp[l] = 0;
+        O m = KT::ORD_INF;
+#pragma unroll
+        for (int j = 0; j < MAX_NB / 32; ++j) {
+            const int b = lane * per + j;
+            if (j < per && b < NB) {
+                if (b >= lo_b && b < mid_b) {
+                    c += bc[j];
+#pragma unroll
+                    for (int l = 0; l < L; ++l) wp[l] += bw[j][l];
+                }
+                if (b >= mid_b && b < hi_b) m = bm[j] < m ? bm[j] : m;
+            }
+        }
+        c = warp_sum_u64(c);
+#pragma unroll
+        for (int l = 0; l < L; ++l) wp[l] = warp_sum_u64(wp[l]);
+        m = warp_min_ord<O>(m);
+        const uint64_t count = cnt_below + c;
+        uint64_t wacc[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) wacc[l] = w_below[l] + wp[l];
+        const O kminO = m < kmin_above ? m : kmin_above;
+        const K t = KT::mid(lo, hi);
+        const K kmin = KT::unord(kminO);
+        const K dist = kmin - t;
+        ++steps;
+        if (!(dist < KT::inf())) {
+            // no item on the right of t (recursive_bisection.rs:522-545)
+            if (prev == count) {
+                state = SEG_ALLLEFT;
+                split_pos = hi;
+                wl_out = sum;
+                nleft = sg.n;
+                break;
+            }
+            hi = t;
+            prev = count;
+            hi_b = mid_b;
+            kmin_above = kminO;
+            continue;
+        }
+        const V wl = WT::value(wacc, fs);
+        const double ideal = WT::f64(sum) / 2.0;
+        const double imb = fabs((WT::f64(wl) - ideal) / ideal);
+        if (count == prev || hi <= t + dist || imb <= tol) {
+            state = SEG_DONE;
+            pivot = kmin;
+            split_pos = t;
+            wl_out = wl;
+            nleft = count;
+            break;
+        }
+        prev = count;
+        if (WT::less(wl, WT::sub(sum, wl))) {
+            lo = t;
+            lo_b = mid_b;
+            cnt_below = count;
+#pragma unroll
+            for (int l = 0; l < L; ++l) w_below[l] = wacc[l];
+        } else {
+            hi = t;
+            hi_b = mid_b;
+            kmin_above = kminO;
+        }
+    }
+    const uint32_t total_steps = sg.steps + steps;
+    if (state != SEG_ACTIVE) {
+        if (lane == 0) {
+            Seg<KT> &o = segs[s];
+            o.state = state;
+            o.pivot = pivot;
+            o.split_pos = split_pos;
+            o.wl = WT::bits(wl_out);
+            o.nleft = (uint32_t)nleft;
+            o.steps = total_steps;
+            o.lo = lo;
+            o.hi = hi;
+            o.prev = prev;
+            flags[k] = 0;
+            atomicAdd((unsigned long long *)&rs->steps_total, (unsigned long long)total_steps);
+            atomicMax((unsigned long long *)&rs->steps_max, (unsigned long long)total_steps);
+            atomicAdd((unsigned long long *)&rs->splits, 1ull);
+        }
+    } else {
+        // keep searching: clear this segment's bins for the next pass
+#pragma unroll
+        for (int j = 0; j < MAX_NB / 32; ++j) {
+            const int b = lane * per + j;
+            if (j < per && b < NB) {
+                const size_t g = (size_t)s * NB + b;
+                H.cnt[g] = 0;
+#pragma unroll
+                for (int l = 0; l < L; ++l) H.w[g * L + l] = 0;
+                H.inv[g] = 0;
+            }
+        }
+        if (lane == 0) {
+            Seg<KT> &o = segs[s];
+            o.lo = lo;
+            o.hi = hi;
+            o.prev = prev;
+            o.steps = total_steps;
+            flags[k] = 1;
+        }
+    }
+}
+
+// Compacts the listed segments still searching into list2 with the exclusive
+// prefix P2 of their sizes.  One CTA.
+template <class KT>
+__global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+                                                    const uint32_t *__restrict__ flags, uint32_t nlist,
+                                                    uint32_t *list2, uint64_t *P2, RunScalars *rs) {
+    __shared__ uint64_t sh[33];
+    uint64_t outc = 0, run = 0;
+    for (uint32_t base = 0; base < nlist; base += blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        const bool keep = k < nlist && flags[k];
+        const uint32_t s = keep ? list[k] : 0;
+        const uint64_t sz = keep ? segs[s].n : 0;
+        uint64_t tc, tp;
+        const uint64_t ci = block_exscan_u64(keep ? 1 : 0, sh, tc);
+        const uint64_t pi = block_exscan_u64(sz, sh, tp);
+        if (keep) {
+            list2[outc + ci] = s;
+            P2[outc + ci] = run + pi;
+        }
+        outc += tc;
+        run += tp;
+    }
+    if (threadIdx.x == 0) {
+        P2[outc] = run;
+        rs->nactive = outc;
+        rs->total_active = run;
+    }
+}
+
+// Builds the next level's segments from the finished splits: left child
+// (heap 2h+1, sum = weight_left, bbox max[coord] = split_pos) and right child
+// (2h+2, sum - weight_left, bbox min[coord] = split_pos), empty children
+// dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
+// the smallest heap id among the children (the id offset, :698-702).
+template <class KT, class WT>
+__global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ segs, uint32_t S, int coord, int D,
+                                                   int write, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
+                                                   uint64_t n_total, RunScalars *rs) {
+    typedef typename KT::T K;
+    __shared__ uint64_t sh[33];
+    uint64_t outc = 0;
+    uint64_t hmin = ~0ull;
+    const int nc = (coord + 1) % D;
+    for (uint32_t base = 0; base < S; base += blockDim.x) {
+        const uint32_t s = base + threadIdx.x;
+        Seg<KT> sg;
+        uint32_t nl = 0, nr = 0;
+        if (s < S) {
+            sg = segs[s];
+            nl = sg.nleft;
+            nr = sg.n - sg.nleft;
+        }
+        uint64_t tc;
+        const uint64_t ci = block_exscan_u64((nl > 0) + (nr > 0), sh, tc);
+        if (s < S) {
+            const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
+            if (nl > 0) hmin = hl < hmin ? hl : hmin;
+            if (nr > 0) hmin = hr < hmin ? hr : hmin;
+            if (write) {
+                uint64_t c = outc + ci;
+                const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
+                for (int side = 0; side < 2; ++side) {
+                    const uint32_t cn = side == 0 ? nl : nr;
+                    if (!cn) continue;
+                    Seg<KT> ch;
+                    ch.off = side == 0 ? sg.off : sg.off + nl;
+                    ch.heap = side == 0 ? hl : hr;
+                    ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
+                    ch.prev = ~0ull;
+                    ch.wl = 0;
+                    ch.n = cn;
+                    ch.nleft = 0;
+                    ch.state = SEG_ACTIVE;
+                    ch.steps = 0;
+                    for (int d = 0; d < 3; ++d) {
+                        ch.bmin[d] = sg.bmin[d];
+                        ch.bmax[d] = sg.bmax[d];
+                    }
+                    if (side == 0)
+                        ch.bmax[coord] = sg.split_pos;
+                    else
+                        ch.bmin[coord] = sg.split_pos;
+                    ch.lo = ch.bmin[nc];
+                    ch.hi = ch.bmax[nc];
+                    ch.pivot = 0;
+                    ch.split_pos = 0;
+                    next[c] = ch;
+                    next_list[c] = (uint32_t)c;
+                    next_P[c] = ch.off;
+                    ++c;
+                }
+            }
+        }
+        outc += tc;
+    }
+    hmin = warp_min_u64(hmin);
+    if (!write && (threadIdx.x & 31) == 0) atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
+    if (threadIdx.x == 0) {
+        rs->nsegs_next = outc;
+        if (write) next_P[outc] = n_total;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_reorder: stable two-way partition of every segment of the level, out of
+// place, one dynamic chunk of the item range per CTA at a time.  A chunk
+// learns how many left items of its first segment precede it by a decoupled
+// look-back over the chunks before it (bounded wait).
+// ---------------------------------------------------------------------------
+template <int D, class KT, class WT>
+struct ReorderArgs {
+    const Seg<KT> *segs;
+    uint32_t S;
+    uint64_t n;
+    uint64_t chunk;
+    uint64_t nchunks;
+    int coord;
+    const typename KT::T *ksrc[3];
+    typename KT::T *kdst[3];
+    const typename WT::S *wsrc;
+    typename WT::S *wdst;
+    const uint32_t *isrc;  // NULL: identity
+    uint32_t *idst;
+    uint64_t *lb;  // look-back words, one per chunk, zeroed
+    RunScalars *rs;
+};
+
+template <class KT>
+__device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg) {
+    return sg.state == SEG_ALLLEFT || key < sg.pivot;
+}
+
+template <class T>
+__device__ __forceinline__ void stage_out(const T *stage, T *dst, uint32_t tcount, uint32_t tile_left, uint64_t left_base,
+                                          uint64_t right_base, uint64_t seg_end, uint64_t left_end, RunScalars *rs) {
+    for (uint32_t k = threadIdx.x; k < tcount; k += BLOCK) {
+        uint64_t d = k < tile_left ? left_base + k : right_base + (k - tile_left);
+        bool ok = k < tile_left ? d < left_end : (d >= left_end && d < seg_end);
+        if (ok)
+            dst[d] = stage[k];
+        else
+            atomicOr(&rs->err, ERR_SCATTER_BOUNDS);
+    }
+}
+
+template <int D, class KT, class WT>
+__global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
+    typedef typename KT::T K;
+    __shared__ uint64_t stage_raw[R_TILE];
+    __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
+    __shared__ uint64_t sh[33];
+    __shared__ uint64_t s_ticket, s_prefix;
+    __shared__ uint32_t s_fail;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const K *__restrict__ kc = A.ksrc[A.coord];
+    for (;;) {
+        if (threadIdx.x == 0) s_ticket = atomicAdd((unsigned long long *)&A.rs->ticket, 1ull);
+        __syncthreads();
+        const uint64_t t = s_ticket;
+        if (t >= A.nchunks) break;
+        const uint64_t c0 = t * A.chunk, c1 = min(A.n, c0 + A.chunk);
+        const uint32_t kf = seg_index_of<KT>(A.segs, A.S, c0);
+        const uint32_t kl = seg_index_of<KT>(A.segs, A.S, c1 - 1);
+        // count the left items of the last piece
+        const Seg<KT> sl = A.segs[kl];
+        const uint64_t la = max(c0, sl.off);
+        uint64_t cnt = 0;
+        for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK) cnt += goes_left<KT>(kc[e], sl) ? 1 : 0;
+        uint64_t agg;
+        block_exscan_u64(cnt, sh, agg);
+        const Seg<KT> sf = A.segs[kf];
+        if (threadIdx.x == 0) {
+            const bool last_starts_here = sl.off >= c0;
+            s_fail = 0;
+            if (last_starts_here) atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_INCL | agg));
+            else atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_AGG | agg));
+            uint64_t prefix = 0;
+            if (sf.off < c0) {
+                // look back: chunk t-1 ends inside segment kf
+                int64_t j = (int64_t)t - 1;
+                for (;;) {
+                    uint64_t v;
+                    uint32_t spins = 0;
+                    while ((v = *((volatile uint64_t *)&A.lb[j])) == 0) {
+                        if (++spins > LB_SPIN_LIMIT) break;
+                        __nanosleep(64);
+                    }
+                    if (v == 0) {
+                        atomicOr(&A.rs->err, ERR_LOOKBACK_TIMEOUT);
+                        s_fail = 1;
+                        break;
+                    }
+                    prefix += v & LB_VALUE;
+                    if ((v & ~LB_VALUE) == LB_INCL) break;
+                    if (--j < 0) {
+                        atomicOr(&A.rs->err, ERR_LOOKBACK_TIMEOUT);
+                        s_fail = 1;
+                        break;
+                    }
+                }
+                if (!last_starts_here)
+                    atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_INCL | ((prefix + agg) & LB_VALUE)));
+            }
+            s_prefix = prefix;
+        }
+        __syncthreads();
+        if (s_fail) continue;
+        const uint64_t prefix_first = s_prefix;
+        for (uint32_t kk = kf; kk <= kl; ++kk) {
+            const Seg<KT> sg = A.segs[kk];
+            const uint64_t pa = max(c0, sg.off), pb = min(c1, sg.off + sg.n);
+            uint64_t running = kk == kf ? prefix_first : 0;
+            const uint64_t seg_end = sg.off + sg.n, left_end = sg.off + sg.nleft;
+            for (uint64_t ts = pa; ts < pb; ts += R_TILE) {
+                const uint32_t tcount = (uint32_t)min((uint64_t)R_TILE, pb - ts);
+                bool fl[R_ITEMS];
+                uint32_t bal[R_ITEMS];
+#pragma unroll
+                for (int i = 0; i < R_ITEMS; ++i) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    const bool valid = li < tcount;
+                    const K key = valid ? kc[ts + li] : (K)0;
+                    fl[i] = valid && goes_left<KT>(key, sg);
+                    bal[i] = __ballot_sync(0xffffffffu, fl[i]);
+                    if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
+                }
+                __syncthreads();
+                if (warp == 0) {
+                    // exclusive scan of R_ITEMS * NWARPS counts in (row, warp) order
+                    constexpr int PER = (R_ITEMS * NWARPS + 31) / 32;
+                    uint32_t v[PER], tot = 0;
+#pragma unroll
+                    for (int j = 0; j < PER; ++j) {
+                        const int idx = lane * PER + j;
+                        v[j] = idx < R_ITEMS * NWARPS ? s_cnt[idx] : 0;
+                        tot += v[j];
+                    }
+                    uint32_t inc = tot;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+                        if (lane >= o) inc += u;
+                    }
+                    uint32_t run = inc - tot;
+#pragma unroll
+                    for (int j = 0; j < PER; ++j) {
+                        const int idx = lane * PER + j;
+                        if (idx < R_ITEMS * NWARPS) s_cnt[idx] = run;
+                        run += v[j];
+                    }
+                    if (lane == 31) sh[0] = inc;
+                }
+                __syncthreads();
+                const uint32_t tile_left = (uint32_t)sh[0];
+                uint16_t pos[R_ITEMS];
+#pragma unroll
+                for (int i = 0; i < R_ITEMS; ++i) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & ((1u << lane) - 1));
+                    pos[i] = (uint16_t)(fl[i] ? before : tile_left + (li - before));
+                }
+                const uint64_t left_base = sg.off + running;
+                const uint64_t right_base = sg.off + sg.nleft + (ts - sg.off - running);
+                // keys
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    K *st = (K *)stage_raw;
+#pragma unroll
+                    for (int i = 0; i < R_ITEMS; ++i) {
+                        const uint32_t li = i * BLOCK + threadIdx.x;
+                        if (li < tcount) st[pos[i]] = A.ksrc[d][ts + li];
+                    }
+                    __syncthreads();
+                    stage_out<K>(st, A.kdst[d], tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                    __syncthreads();
+                }
+                {
+                    typedef typename WT::S WS;
+                    WS *st = (WS *)stage_raw;
+#pragma unroll
+                    for (int i = 0; i < R_ITEMS; ++i) {
+                        const uint32_t li = i * BLOCK + threadIdx.x;
+                        if (li < tcount) st[pos[i]] = A.wsrc[ts + li];
+                    }
+                    __syncthreads();
+                    stage_out<WS>(st, A.wdst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                    __syncthreads();
+                }
+                {
+                    uint32_t *st = (uint32_t *)stage_raw;
+#pragma unroll
+                    for (int i = 0; i < R_ITEMS; ++i) {
+                        const uint32_t li = i * BLOCK + threadIdx.x;
+                        if (li < tcount) st[pos[i]] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
+                    }
+                    __syncthreads();
+                    stage_out<uint32_t>(st, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                    __syncthreads();
+                }
+                running += tile_left;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_assign: last level — part id of every item = heap id of its leaf minus
+// the smallest heap id (recursive_bisection.rs:589-601, 698-702).
+// ---------------------------------------------------------------------------
+template <class KT>
+__global__ void __launch_bounds__(BLOCK) k_assign(const Seg<KT> *__restrict__ segs, uint32_t S, uint64_t n,
+                                                  const typename KT::T *__restrict__ kc, const uint32_t *__restrict__ isrc,
+                                                  uint64_t *__restrict__ part, RunScalars *rs) {
+    const uint64_t c0 = n * blockIdx.x / gridDim.x, c1 = n * (blockIdx.x + 1) / gridDim.x;
+    if (c0 >= c1) return;
+    const uint64_t hmin = rs->min_heap;
+    uint32_t k = seg_index_of<KT>(segs, S, c0);
+    uint64_t pos = c0;
+    while (pos < c1) {
+        const Seg<KT> sg = segs[k];
+        const uint64_t pe = min(c1, sg.off + sg.n);
+        const uint64_t hl = 2 * sg.heap + 1 - hmin, hr = 2 * sg.heap + 2 - hmin;
+        for (uint64_t e = pos + threadIdx.x; e < pe; e += BLOCK) {
+            const uint64_t id = goes_left<KT>(kc[e], sg) ? hl : hr;
+            const uint64_t dst = isrc ? isrc[e] : e;
+            if (dst < n)
+                part[dst] = id;
+            else
+                atomicOr(&rs->err, ERR_SCATTER_BOUNDS);
+        }
+        pos = pe;
+        ++k;
+    }
+}
+
+static __global__ void k_fill_u64(uint64_t *p, uint64_t n, uint64_t v) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+}  // namespace cg

@@ -1,0 +1,293 @@
+// The level loop of one Rcb run (host side), templated on dimension, key
+// precision and weight type.  It replaces rcb / rcb_recurse
+// (coupe/src/algorithms/recursive_bisection.rs:575-705): instead of a
+// fork-join over the bisection tree, every tree level is processed at once,
+// all of its segments in the same kernel launches.
+#pragma once
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "engine.h"
+#include "kernels.cuh"
+
+namespace cg {
+
+#define CG_CK(call)                                               \
+    do {                                                          \
+        cudaError_t e_ = (call);                                  \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call, err);  \
+    } while (0)
+
+#define CG_LAUNCHED()                                             \
+    do {                                                          \
+        cudaError_t e_ = cudaGetLastError();                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, "launch", err); \
+        ++st->kernel_launches;                                    \
+    } while (0)
+
+struct Bump {
+    char *base;
+    size_t off;
+    template <class T>
+    T *take(size_t count) {
+        off = (off + 255) & ~(size_t)255;
+        T *p = (T *)(base + off);
+        off += count * sizeof(T);
+        return p;
+    }
+};
+
+template <int D, class KT, class WT>
+struct Buffers {
+    typedef typename KT::T K;
+    typedef typename KT::Ord O;
+    K *keys[2][3];
+    typename WT::S *w[2];
+    uint32_t *idx[2];
+    Seg<KT> *segs[2];
+    uint32_t *list[2];
+    uint64_t *P[2];
+    uint32_t *flags;
+    uint32_t *hcnt;
+    uint64_t *hw;
+    O *hinv;
+    uint64_t *lb;
+    RunScalars *rs;
+    uint64_t hist_bins;
+    uint64_t lb_cap;
+
+    size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap) {
+        for (int s = 0; s < 2; ++s) {
+            for (int d = 0; d < 3; ++d) keys[s][d] = d < D ? b.take<K>(n) : nullptr;
+            w[s] = b.take<typename WT::S>(n);
+            idx[s] = b.take<uint32_t>(n);
+            segs[s] = b.take<Seg<KT>>(scap);
+            list[s] = b.take<uint32_t>(scap);
+            P[s] = b.take<uint64_t>(scap + 1);
+        }
+        flags = b.take<uint32_t>(scap);
+        hcnt = b.take<uint32_t>(hb);
+        hw = b.take<uint64_t>(hb * WT::LIMBS);
+        hinv = b.take<O>(hb);
+        lb = b.take<uint64_t>(lbcap);
+        rs = b.take<RunScalars>(1);
+        hist_bins = hb;
+        lb_cap = lbcap;
+        return b.off;
+    }
+};
+
+static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem) {
+    int per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fn, block, smem) != cudaSuccess || per < 1) per = 1;
+    return per * sms;
+}
+
+template <int D, class KT, class WT>
+int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
+    typedef typename KT::T K;
+    const uint64_t n = a.n;
+    cudaStream_t s = a.stream ? a.stream : C.stream;
+    st->points = n;
+    if (n == 0) return COUPE_ERR_OK;
+    if (n > 0xffffffffull) {
+        *err = "more than 2^32 - 1 points";
+        return COUPE_ERR_ALLOC;
+    }
+    if (a.iter_count == 0) {
+        // rcb_recurse with iter_count == 0 stores id 0 everywhere (:589-602)
+        k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part, n, 0);
+        CG_LAUNCHED();
+        CG_CK(cudaStreamSynchronize(s));
+        return COUPE_ERR_OK;
+    }
+    // segment capacity: a level holds at most min(2^level, n) segments
+    uint64_t scap = a.iter_count >= 40 ? n : std::min<uint64_t>(n, 1ull << a.iter_count);
+    scap = std::max<uint64_t>(scap, 1);
+    const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
+    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, 0);
+    uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * 4 - 1) / ((uint64_t)g_reorder * 4));
+    chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
+    const uint64_t nchunks = (n + chunk - 1) / chunk;
+
+    Buffers<D, KT, WT> B;
+    Bump dry{nullptr, 0};
+    const size_t need = B.carve(dry, n, scap, hb, nchunks);
+    int rc = ensure_workspace(C, need, err);
+    if (rc != COUPE_ERR_OK) return rc;
+    Bump real{(char *)C.ws, 0};
+    B.carve(real, n, scap, hb, nchunks);
+    RunScalars *h_rs = (RunScalars *)C.h_pinned;
+
+    const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
+    const int g_hist = occupancy_grid((const void *)k_hist<KT, WT>, C.sms, BLOCK, 0);
+
+    CG_CK(cudaEventRecord(C.ev0, s));
+    RunScalars init;
+    std::memset(&init, 0, sizeof(init));
+    for (int d = 0; d < 3; ++d) {
+        init.bbox_min_ord[d] = ord_f64(1.7976931348623157e308);
+        init.bbox_max_ord[d] = ord_f64(-1.7976931348623157e308);
+    }
+    init.min_heap = ~0ull;
+    *h_rs = init;
+    CG_CK(cudaMemcpyAsync(B.rs, h_rs, sizeof(RunScalars), cudaMemcpyHostToDevice, s));
+
+    Mat M;
+    std::memset(&M, 0, sizeof(M));
+    M.on = a.has_matrix ? 1 : 0;
+    for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
+    k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2], B.rs);
+    CG_LAUNCHED();
+    const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
+    if (WT::LIMBS > 1) {
+        k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs);
+        CG_LAUNCHED();
+    }
+    k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs);
+    CG_LAUNCHED();
+    k_root<KT, WT><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs);
+    CG_LAUNCHED();
+
+    // algorithmic bytes: the input read and the SoA keys written
+    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
+    uint64_t bytes = n * (D * 8 + sw) + n * D * sk + n * sw;  // convert + weight sum
+    if (WT::LIMBS > 1) bytes += n * sw;
+
+    int cur = 0;       // buffers of the current level
+    bool w_user = true;  // level 0 reads the caller's weights and implicit indices
+    uint64_t S = 1;
+    for (uint64_t L = 0; L < a.iter_count; ++L) {
+        const int coord = (int)(L % D);
+        // bins per segment: as many bisection steps per pass as the budget allows
+        int nbk = MAX_NBK;
+        while (nbk > 1 && S * (1ull << nbk) > B.hist_bins) --nbk;
+        const uint64_t NB = 1ull << nbk;
+        Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
+        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
+        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
+        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
+        const K *kc = B.keys[cur][coord];
+        const typename WT::S *wc = w_user ? w_in : B.w[cur];
+        const uint32_t *ic = w_user ? nullptr : B.idx[cur];
+        Seg<KT> *segs = B.segs[cur];
+        int li = 0;  // list / P buffer in use
+        uint64_t nlist = S;
+        k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk, n, B.rs);
+        CG_LAUNCHED();
+        ++st->hist_passes;
+        st->hist_points += n;
+        bytes += n * (sk + sw);
+        for (;;) {
+            k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(segs, B.list[li], (uint32_t)nlist, H,
+                                                                                      nbk, a.tolerance, B.flags, B.rs);
+            CG_LAUNCHED();
+            k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1], B.P[li ^ 1], B.rs);
+            CG_LAUNCHED();
+            CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+            CG_CK(cudaStreamSynchronize(s));
+            if (h_rs->err) break;
+            if (h_rs->nactive == 0) break;
+            li ^= 1;
+            nlist = h_rs->nactive;
+            k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk, n, B.rs);
+            CG_LAUNCHED();
+            ++st->hist_passes;
+            st->hist_points += h_rs->total_active;
+            bytes += h_rs->total_active * (sk + sw);
+        }
+        if (h_rs->err) break;
+        const bool last = L + 1 == a.iter_count;
+        const int nxt = cur ^ 1;
+        k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[nxt], B.list[0], B.P[0], n,
+                                             B.rs);
+        CG_LAUNCHED();
+        if (last) {
+            k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs);
+            CG_LAUNCHED();
+            bytes += n * (sk + (ic ? 4 : 0) + 8);
+            st->levels = L + 1;
+            break;
+        }
+        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+        CG_CK(cudaStreamSynchronize(s));
+        if (h_rs->err) break;
+        const uint64_t S_next = h_rs->nsegs_next;
+        CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
+        CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
+        ReorderArgs<D, KT, WT> R;
+        R.segs = segs;
+        R.S = (uint32_t)S;
+        R.n = n;
+        R.chunk = chunk;
+        R.nchunks = nchunks;
+        R.coord = coord;
+        for (int d = 0; d < 3; ++d) {
+            R.ksrc[d] = B.keys[cur][d];
+            R.kdst[d] = B.keys[nxt][d];
+        }
+        R.wsrc = wc;
+        R.wdst = B.w[nxt];
+        R.isrc = ic;
+        R.idst = B.idx[nxt];
+        R.lb = B.lb;
+        R.rs = B.rs;
+        k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, 0, s>>>(R);
+        CG_LAUNCHED();
+        bytes += n * sk /* flag pre-count */ + 2 * n * (D * sk + sw + 4) - (ic ? 0 : n * 4);
+        cur = nxt;
+        w_user = false;
+        S = S_next;
+        st->levels = L + 1;
+    }
+    CG_CK(cudaEventRecord(C.ev1, s));
+    CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+    CG_CK(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, C.ev0, C.ev1);
+    st->device_ms = ms;
+    st->splits = h_rs->splits;
+    st->split_steps = h_rs->steps_total;
+    st->max_split_steps = h_rs->steps_max;
+    st->fixed_scale = h_rs->fscale;
+    {
+        uint64_t lim[4] = {h_rs->wsum_limbs[0], h_rs->wsum_limbs[1], h_rs->wsum_limbs[2], h_rs->wsum_limbs[3]};
+        st->root_weight_sum = WT::f64(WT::value(lim, h_rs->fscale));
+    }
+    st->algo_bytes = bytes;
+    if (h_rs->err) {
+        uint32_t e = h_rs->err;
+        if (e & ERR_NONFINITE_WEIGHT) {
+            *err = "f64 weights must be finite";
+            return COUPE_ERR_BAD_TYPE;
+        }
+        *err = std::string("device check failed (code ") + std::to_string(e) + ")";
+        return COUPE_ERR_CRASH;
+    }
+    return COUPE_ERR_OK;
+}
+
+template <class KT>
+int run_mode(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
+    if (a.dim == 2) {
+        switch (a.wtype) {
+        case 0: return run_typed<2, KT, WtI32>(C, a, st, err);
+        case 1: return run_typed<2, KT, WtI64>(C, a, st, err);
+        case 2: return run_typed<2, KT, WtF64>(C, a, st, err);
+        }
+    } else if (a.dim == 3) {
+        switch (a.wtype) {
+        case 0: return run_typed<3, KT, WtI32>(C, a, st, err);
+        case 1: return run_typed<3, KT, WtI64>(C, a, st, err);
+        case 2: return run_typed<3, KT, WtF64>(C, a, st, err);
+        }
+    } else {
+        return COUPE_ERR_BAD_DIMENSION;
+    }
+    *err = "unknown weight type";
+    return COUPE_ERR_BAD_TYPE;
+}
+
+}  // namespace cg

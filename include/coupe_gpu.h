@@ -1,0 +1,98 @@
+/*
+ * coupe_gpu.h — entry points of libcoupe_gpu.so beyond coupe's own ABI.
+ *
+ * coupe.h covers the drop-in calls.  The functions here add what a GPU
+ * caller needs and the reference has no counterpart for: device-resident
+ * inputs, the choice of key precision, run statistics and the detailed
+ * message of the last error on the calling thread.
+ */
+#ifndef COUPE_GPU_H
+#define COUPE_GPU_H
+
+#include <stdint.h>
+#include "coupe.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Key precision of the split search.
+ * COUPE_GPU_REF32: coupe's arithmetic — f32 keys, f32 cuts, f32 distances
+ *   (coupe/src/algorithms/recursive_bisection.rs:472-555, 604-616, 674-679).
+ *   Part ids equal coupe::Rcb's for integer weights.  Default of coupe_rcb.
+ * COUPE_GPU_F64: the same algorithm with f64 keys, cuts and split positions.
+ * COUPE_GPU_F32KEY_F64BAND: f32 keys streamed, with every comparison whose
+ *   f32 key cannot decide it re-checked in f64; the result equals
+ *   COUPE_GPU_F64's. */
+enum coupe_gpu_mode {
+	COUPE_GPU_REF32 = 0,
+	COUPE_GPU_F64 = 1,
+	COUPE_GPU_F32KEY_F64BAND = 2,
+};
+
+/* Statistics of the last run on the calling thread. */
+struct coupe_gpu_stats {
+	uint64_t points;          /* N */
+	uint64_t levels;          /* tree levels processed */
+	uint64_t splits;          /* non-empty segments split */
+	uint64_t split_steps;     /* bisection steps, summed over splits */
+	uint64_t max_split_steps; /* most steps of one split */
+	uint64_t hist_passes;     /* histogram passes launched */
+	uint64_t hist_points;     /* points read by histogram passes */
+	uint64_t band_points;     /* points re-checked in f64 (band mode) */
+	uint64_t kernel_launches; /* kernels launched by the run */
+	uint64_t algo_bytes;      /* algorithmic HBM bytes of the run */
+	double root_weight_sum;   /* total weight as f64 */
+	double device_ms;         /* device time of the run (CUDA events) */
+	int fixed_scale;          /* s of the 128-bit fixed-point weight sums */
+	int mode;                 /* enum coupe_gpu_mode used */
+};
+
+/* coupe_rcb with an explicit precision mode. */
+enum coupe_err coupe_gpu_rcb(uintptr_t *partition, uintptr_t dimension,
+		const coupe_data *points, const coupe_data *weights,
+		uintptr_t iter_count, double tolerance, int mode);
+
+/* coupe_rib with an explicit precision mode. */
+enum coupe_err coupe_gpu_rib(uintptr_t *partition, uintptr_t dimension,
+		const coupe_data *points, const coupe_data *weights,
+		uintptr_t iter_count, double tolerance, int mode);
+
+/* Rcb on device-resident inputs: `d_points` holds n points of `dimension`
+ * doubles (AoS, 8-byte aligned), `d_weights` n elements of `weight_type`,
+ * `d_partition` receives n part ids.  `stream` is a cudaStream_t (NULL: the
+ * library's own stream); the call returns after the work on it completed.
+ * `matrix` (host, dimension x dimension, row-major) may be NULL; when given,
+ * every point p is replaced by matrix * p before the bisection, which is how
+ * Rib applies its basis change. */
+enum coupe_err coupe_gpu_rcb_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
+		const double *d_points, enum coupe_type weight_type, const void *d_weights,
+		uint64_t iter_count, double tolerance, int mode, const double *matrix,
+		void *stream);
+
+/* Rib on device-resident inputs (see coupe_gpu_rcb_device). */
+enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
+		const double *d_points, enum coupe_type weight_type, const void *d_weights,
+		uint64_t iter_count, double tolerance, int mode, void *stream);
+
+/* The Rib basis change of n device-resident points: writes obb_to_aabb
+ * (host, dimension x dimension, row-major), the inverse of the Householder
+ * reflection that maps the first axis onto the principal inertia axis
+ * (coupe/src/geometry.rs:210-228, 273-319). */
+enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double *d_points,
+		double *obb_to_aabb, void *stream);
+
+/* Copies the statistics of the calling thread's last run. */
+void coupe_gpu_last_stats(struct coupe_gpu_stats *out);
+
+/* Detailed message of the calling thread's last error ("" if none). */
+const char *coupe_gpu_last_error(void);
+
+/* Library version string. */
+const char *coupe_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COUPE_GPU_H */

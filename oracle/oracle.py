@@ -1,0 +1,184 @@
+"""TEST INFRASTRUCTURE ONLY — ctypes wrapper of the oracle (rcb_oracle.cpp).
+
+The oracle is a CPU restatement of coupe's Rcb / Rib used by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.  The
+product never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PATH = os.path.join(HERE, "build", "liboracle_rcb.so")
+
+REF32, F64 = 0, 1
+FSUM_SEQ, FSUM_FIXED = 0, 1
+_WT = {np.dtype(np.int32): 0, np.dtype(np.int64): 1, np.dtype(np.float64): 2}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("splits", ctypes.c_uint64), ("iterations", ctypes.c_uint64),
+                ("max_iterations", ctypes.c_uint64), ("pivot_ties", ctypes.c_uint64),
+                ("active_points", ctypes.c_uint64), ("root_sum", ctypes.c_double),
+                ("fixed_scale", ctypes.c_int), ("pad", ctypes.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "pad"}
+
+
+_lib = None
+
+
+def build():
+    r = subprocess.run(["make", "-s", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    return PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(PATH):
+            build()
+        L = ctypes.CDLL(PATH)
+        vp, u64, i32, dbl = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_double
+        L.oracle_rcb.argtypes = [vp, u64, i32, vp, i32, vp, u64, dbl, i32, i32, i32, ctypes.POINTER(Stats)]
+        L.oracle_rcb.restype = i32
+        L.oracle_rib.argtypes = [vp, u64, i32, vp, i32, vp, u64, dbl, i32, i32, i32, vp, ctypes.POINTER(Stats)]
+        L.oracle_rib.restype = i32
+        L.oracle_rib_matrix.argtypes = [u64, i32, vp, vp]
+        L.oracle_rib_matrix.restype = i32
+        L.oracle_map_points.argtypes = [vp, u64, i32, vp, vp]
+        L.oracle_bbox.argtypes = [vp, u64, i32, vp, vp]
+        L.oracle_inertia_matrix.argtypes = [vp, u64, i32, vp]
+        L.oracle_inertia_vector.argtypes = [vp, i32, vp]
+        L.oracle_householder.argtypes = [vp, i32, vp]
+        L.oracle_fixed_scale.argtypes = [vp, u64]
+        L.oracle_fixed_scale.restype = i32
+        L.oracle_fixed_sum.argtypes = [vp, u64, i32]
+        L.oracle_fixed_sum.restype = dbl
+        L.oracle_split_f32_u32.argtypes = [vp, vp, u64, dbl, ctypes.c_float, ctypes.c_float, vp, vp]
+        L.oracle_split_f32_u32.restype = u64
+        L.oracle_reorder_split_f32.argtypes = [vp, u64, u64]
+        L.oracle_reorder_split_f32.restype = u64
+        _lib = L
+    return _lib
+
+
+def _prep(points, weights):
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    w = np.asarray(weights)
+    if w.dtype.kind in "iu" and w.dtype != np.int32:
+        w = w.astype(np.int64)
+    elif w.dtype.kind == "f":
+        w = w.astype(np.float64)
+    return p, np.ascontiguousarray(w)
+
+
+def rcb(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1):
+    """Part ids (uint64) of coupe's Rcb, and run statistics."""
+    p, w = _prep(points, weights)
+    n, dim = p.shape
+    out = np.zeros(n, dtype=np.uint64)
+    st = Stats()
+    rc = lib().oracle_rcb(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
+                          iter_count, tolerance, mode, fsum, threads, ctypes.byref(st))
+    if rc != 0:
+        raise ValueError("oracle_rcb failed (%d)" % rc)
+    return out, st.as_dict()
+
+
+def rib(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1, matrix=None):
+    p, w = _prep(points, weights)
+    n, dim = p.shape
+    out = np.zeros(n, dtype=np.uint64)
+    st = Stats()
+    m = None if matrix is None else np.ascontiguousarray(np.asarray(matrix, dtype=np.float64))
+    rc = lib().oracle_rib(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
+                          iter_count, tolerance, mode, fsum, threads,
+                          m.ctypes.data if m is not None else None, ctypes.byref(st))
+    if rc != 0:
+        raise ValueError("oracle_rib failed (%d)" % rc)
+    return out, st.as_dict()
+
+
+def rib_matrix(points):
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    n, dim = p.shape
+    m = np.zeros((dim, dim))
+    rc = lib().oracle_rib_matrix(n, dim, p.ctypes.data, m.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle_rib_matrix failed (%d)" % rc)
+    return m
+
+
+def map_points(points, matrix):
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    n, dim = p.shape
+    m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float64))
+    out = np.zeros_like(p)
+    lib().oracle_map_points(p.ctypes.data, n, dim, m.ctypes.data, out.ctypes.data)
+    return out
+
+
+def bbox(points):
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    n, dim = p.shape
+    lo, hi = np.zeros(dim), np.zeros(dim)
+    lib().oracle_bbox(p.ctypes.data, n, dim, lo.ctypes.data, hi.ctypes.data)
+    return lo, hi
+
+
+def inertia_matrix(points):
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    n, dim = p.shape
+    m = np.zeros((dim, dim))
+    lib().oracle_inertia_matrix(p.ctypes.data, n, dim, m.ctypes.data)
+    return m
+
+
+def inertia_vector(m):
+    m = np.ascontiguousarray(np.asarray(m, dtype=np.float64))
+    dim = m.shape[0]
+    v = np.zeros(dim)
+    lib().oracle_inertia_vector(m.ctypes.data, dim, v.ctypes.data)
+    return v
+
+
+def householder(v):
+    v = np.ascontiguousarray(np.asarray(v, dtype=np.float64))
+    dim = v.shape[0]
+    h = np.zeros((dim, dim))
+    lib().oracle_householder(v.ctypes.data, dim, h.ctypes.data)
+    return h
+
+
+def fixed_scale(w):
+    w = np.ascontiguousarray(np.asarray(w, dtype=np.float64))
+    return lib().oracle_fixed_scale(w.ctypes.data, len(w))
+
+
+def fixed_sum(w, s):
+    w = np.ascontiguousarray(np.asarray(w, dtype=np.float64))
+    return lib().oracle_fixed_sum(w.ctypes.data, len(w), s)
+
+
+def split_f32_u32(keys, weights, tolerance, mn, mx):
+    """One par_rcb_split on 1-D keys; returns (left keys, right keys,
+    left weights, right weights, weight_left, split_pos)."""
+    k = np.ascontiguousarray(np.asarray(keys, dtype=np.float32)).copy()
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.uint32)).copy()
+    wl = ctypes.c_uint32()
+    sp = ctypes.c_float()
+    nl = lib().oracle_split_f32_u32(k.ctypes.data, w.ctypes.data, len(k), tolerance, mn, mx,
+                                    ctypes.byref(wl), ctypes.byref(sp))
+    return k[:nl], k[nl:], w[:nl], w[nl:], wl.value, sp.value
+
+
+def reorder_split_f32(keys, pivot_index):
+    k = np.ascontiguousarray(np.asarray(keys, dtype=np.float32)).copy()
+    nl = lib().oracle_reorder_split_f32(k.ctypes.data, len(k), pivot_index)
+    return k[:nl], k[nl:]

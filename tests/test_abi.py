@@ -1,0 +1,88 @@
+"""CPU checks of the C ABI: the library loads without a GPU, exports every
+symbol the headers declare, and validates arguments like coupe-ffi before
+touching the device (coupe-ffi/src/lib.rs:272-304)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for h in ("coupe.h", "coupe_gpu.h"):
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"\b(coupe_\w+)\s*\(", src)
+    return sorted(set(names))
+
+
+def test_exports_every_declared_symbol(coupe):
+    L = coupe.lib()
+    declared = _declared()
+    assert "coupe_rcb" in declared and "coupe_rib" in declared
+    for name in declared:
+        assert hasattr(L, name), name
+    assert sorted(declared) == sorted(coupe.EXPORTED)
+
+
+def test_strerror_matches_reference_messages(coupe):
+    L = coupe.lib()
+    # coupe-ffi/src/lib.rs:69-110
+    assert L.coupe_strerror(0) == b"success"
+    assert L.coupe_strerror(1) == b"allocation failed"
+    assert L.coupe_strerror(3) == b"this algorithm does not support the given mesh dimension"
+    assert L.coupe_strerror(6) == b"input iters (e.g. weights and points) don't have the same length"
+
+
+def _data(L, coupe, arr, t):
+    return L.coupe_data_array(len(arr), t, arr.ctypes.data)
+
+
+def test_len_mismatch_before_bad_dimension(coupe):
+    """A length mismatch is reported first, even with a bad dimension."""
+    L = coupe.lib()
+    pts = np.zeros((4, 2))
+    w = np.ones(3, dtype=np.int64)
+    dp, dw = _data(L, coupe, pts, coupe.COUPE_DOUBLE), _data(L, coupe, w, coupe.COUPE_INT64)
+    part = np.zeros(4, dtype=np.uint64)
+    assert L.coupe_rcb(part.ctypes.data, 7, dp, dw, 2, 0.05) == coupe.ERR_LEN_MISMATCH
+    assert L.coupe_rib(part.ctypes.data, 2, dp, dw, 2, 0.05) == coupe.ERR_LEN_MISMATCH
+    L.coupe_data_free(dp)
+    L.coupe_data_free(dw)
+
+
+def test_bad_dimension(coupe):
+    L = coupe.lib()
+    pts = np.zeros((4, 2))
+    w = np.ones(4, dtype=np.int64)
+    dp, dw = _data(L, coupe, pts, coupe.COUPE_DOUBLE), _data(L, coupe, w, coupe.COUPE_INT64)
+    part = np.zeros(4, dtype=np.uint64)
+    for d in (0, 1, 4, 5):
+        assert L.coupe_rcb(part.ctypes.data, d, dp, dw, 2, 0.05) == coupe.ERR_BAD_DIMENSION
+        assert L.coupe_rib(part.ctypes.data, d, dp, dw, 2, 0.05) == coupe.ERR_BAD_DIMENSION
+    L.coupe_data_free(dp)
+    L.coupe_data_free(dw)
+
+
+def test_empty_input_is_ok_and_untouched(coupe):
+    """rcb returns Ok(()) on empty input (recursive_bisection.rs:685-688)."""
+    L = coupe.lib()
+    pts = np.zeros((0, 3))
+    w = np.zeros(0, dtype=np.int64)
+    dp, dw = _data(L, coupe, pts, coupe.COUPE_DOUBLE), _data(L, coupe, w, coupe.COUPE_INT64)
+    sentinel = np.array([7], dtype=np.uint64)
+    assert L.coupe_rcb(sentinel.ctypes.data, 3, dp, dw, 5, 0.05) == coupe.ERR_OK
+    assert sentinel[0] == 7
+    L.coupe_data_free(dp)
+    L.coupe_data_free(dw)
+
+
+def test_data_free_null_is_noop(coupe):
+    coupe.lib().coupe_data_free(None)
+
+
+def test_version(coupe):
+    assert b"sm_103a" in coupe.lib().coupe_gpu_version()
