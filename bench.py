@@ -1,0 +1,349 @@
+"""Benchmark: coupe Rcb on one GB300 (and N replicas under torchrun).
+
+Workload (one "step"): Rcb of 16,777,216 3D points (a mixture of 32 Gaussians)
+with int64 weights U{1..100} into 1024 parts (iter_count 10, tolerance 0.01).
+Inputs are 537 MB per step (larger than the 129 MB L2), so no L2 flush is
+needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value`   device-resident throughput (inputs in HBM before the timed region),
+          Mpoints/s, of the headline precision mode.
+`e2e`     the same metric through the C ABI (coupe_gpu_rcb) with pinned host
+          buffers: host->device copies and the part-id read-back are inside.
+`roofline` the kernel with the largest share of device time, its algorithmic
+          bytes per launch over its CUDA-event duration, against the measured
+          HBM copy bandwidth.
+`cpu_baseline` the CPU restatement of coupe's Rcb (OpenMP, all host cores).
+--impl reference times that CPU restatement alone (the reference itself is
+Rust and cannot be built here).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "RCB Mpoints/s, 16M 3D pts→1024 parts: FP32-key+FP64-band vs plain FP64 on GB300"
+UNIT = "Mpoints/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=16_777_216)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for i, nm in enumerate(names):
+                    if r[5 + i].lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(pts, w, cfg, budget_s=20.0):
+    """The oracle (OpenMP restatement of coupe's rayon Rcb) on all host cores,
+    on the full workload, repeated while the time budget lasts."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    times, ids = [], None
+    t_end = time.perf_counter() + budget_s
+    while True:
+        t0 = time.perf_counter()
+        ids, _ = oracle.rcb(pts, w, cfg["iter_count"], cfg["tolerance"], threads=0)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() + times[-1] > t_end or len(times) >= 5:
+            break
+    t = statistics.median(times)
+    cores = os.cpu_count()
+    return {"value": len(pts) / t / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "full workload (%d points), %d runs, median %.3f s; OpenMP restatement of coupe "
+                      "Rcb (reference is Rust, not buildable here)" % (len(pts), len(times), t)}, ids
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from coupe_gb300 import workloads
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    pts, w, cfg = workloads.gaussian_mixture3d(n=args.points)
+    n = len(pts)
+    # size each step so that the whole run ends within a few minutes
+    t0 = time.perf_counter()
+    oracle.rcb(pts, w, cfg["iter_count"], cfg["tolerance"], threads=0)
+    t_full = time.perf_counter() - t0
+    sample = n
+    if t_full * (args.steps + args.warmup) > 150.0:
+        sample = max(1 << 16, int(n * 150.0 / (t_full * (args.steps + args.warmup))))
+    ps, ws = pts[:sample], w[:sample]
+    for _ in range(max(0, args.warmup - 1)):
+        oracle.rcb(ps, ws, cfg["iter_count"], cfg["tolerance"], threads=0)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.rcb(ps, ws, cfg["iter_count"], cfg["tolerance"], threads=0)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = sample / (ms / 1e3) / 1e6
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": cfg["name"], "points": n, "dim": 3, "parts": 1 << cfg["iter_count"],
+                   "iter_count": cfg["iter_count"], "tolerance": cfg["tolerance"], "weights": "int64 U{1..100}"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d of %d points per step (first points of the seeded workload); OpenMP "
+                                   "restatement of coupe Rcb on all host cores" % (sample, n)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import torch.distributed as dist
+    import coupe_gb300 as coupe
+    from coupe_gb300 import workloads
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    coupe.lib()
+
+    pts_h, w_h, cfg = workloads.gaussian_mixture3d(n=args.points, seed=rank)
+    n = len(pts_h)
+    iters, tol = cfg["iter_count"], cfg["tolerance"]
+    pts = torch.from_numpy(pts_h).to(dev)
+    w = torch.from_numpy(w_h).to(dev)
+    part = torch.empty(n, dtype=torch.int64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    modes = ["ref32", "f64"]
+    if coupe.MODES.get("f32key_f64band") is not None and _mode_available(coupe, pts, w, part):
+        modes.append("f32key_f64band")
+    headline = "f32key_f64band" if "f32key_f64band" in modes else "ref32"
+
+    results, launches, ids_by_mode = {}, {}, {}
+    clocks = None
+    for mode in modes:
+        for _ in range(args.warmup):
+            coupe.rcb_device(part, pts, w, iters, tol, mode=mode)
+        barrier()
+        if mode == headline:
+            clocks = Clocks(local).__enter__()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nl = 0
+        ev0.record(stream)
+        for _ in range(args.steps):
+            coupe.rcb_device(part, pts, w, iters, tol, mode=mode)
+            nl += coupe.last_stats()["kernel_launches"]
+        ev1.record(stream)
+        barrier()
+        if mode == headline:
+            clocks.__exit__()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        results[mode] = ms
+        launches[mode] = nl
+        ids_by_mode[mode] = part.cpu().numpy().view(np.uint64).copy()
+    stats = coupe.last_stats()
+
+    # live roofline: per-kernel CUDA-event times over K more steps
+    coupe.profile(True)
+    for _ in range(args.steps):
+        coupe.rcb_device(part, pts, w, iters, tol, mode=headline)
+    torch.cuda.synchronize()
+    prof = coupe.profile_read()
+    coupe.profile(False)
+    total_ms = sum(v["ms"] for v in prof.values()) or 1.0
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    peak, peak_kind = measured_peak()
+    achieved = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9
+    traffic = _traffic_per_launch(top[0])
+    roofline = {"bound": "hbm", "kernel": top[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": traffic, "algorithmic_bytes_per_launch": top[1]["bytes"] // max(1, top[1]["launches"]),
+                "launches": top[1]["launches"], "share": round(top[1]["ms"] / total_ms, 3),
+                "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                "share": round(v["ms"] / total_ms, 3),
+                                "GBps": round(v["bytes"] / (v["ms"] / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                            for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}
+
+    # end to end through the C ABI, pinned host buffers
+    pin_p = torch.from_numpy(pts_h).pin_memory()
+    pin_w = torch.from_numpy(w_h).pin_memory()
+    pin_o = torch.empty(n, dtype=torch.int64).pin_memory()
+    hp, hw, ho = pin_p.numpy(), pin_w.numpy(), pin_o.numpy().view(np.uint64)
+    rcb = coupe.Rcb(iter_count=iters, tolerance=tol, mode=headline)
+    for _ in range(args.warmup):
+        rcb.partition(ho, (hp, hw))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        rcb.partition(ho, (hp, hw))
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_ok = bool((ho == ids_by_mode[headline]).all())
+
+    cpu = None
+    parity = {}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu, cpu_ids = cpu_baseline(pts_h, w_h, cfg)
+        parity["ref32_vs_oracle_mismatches"] = int((cpu_ids != ids_by_mode["ref32"]).sum())
+    if "f32key_f64band" in ids_by_mode:
+        parity["band_vs_f64_mismatches"] = int((ids_by_mode["f32key_f64band"] != ids_by_mode["f64"]).sum())
+    parity["e2e_ids_equal_device_ids"] = e2e_ok
+
+    ms = results[headline]
+    value = world * n / (ms / 1e3) / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if headline == "f32key_f64band" else "f32",
+        "data": "synthetic",
+        "config": {"workload": cfg["name"], "points": n, "dim": 3, "parts": 1 << iters, "iter_count": iters,
+                   "tolerance": tol, "weights": "int64 U{1..100}", "mode": headline,
+                   "l2": "inputs larger than L2 (%d MB per step), no flush" % ((pts_h.nbytes + w_h.nbytes) >> 20),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "modes": {m: {"ms_per_step": round(results[m], 4), "value": round(world * n / (results[m] / 1e3) / 1e6, 2)}
+                  for m in results},
+        "e2e": {"value": round(world * n / t_e2e / 1e6, 2), "unit": UNIT,
+                "h2d_bytes_per_step": int(pts_h.nbytes + w_h.nbytes), "d2h_bytes_per_step": int(n * 8),
+                "ms_per_step": round(t_e2e * 1e3, 3)},
+        "gpu_launches": launches[headline],
+        "roofline": roofline,
+        "run": {"splits": stats["splits"], "split_steps": stats["split_steps"],
+                "max_split_steps": stats["max_split_steps"], "hist_passes": stats["hist_passes"],
+                "algo_bytes": stats["algo_bytes"], "kernel_launches_per_step": stats["kernel_launches"]},
+        "parity": parity,
+        "clocks": clocks.summary() if clocks else None,
+    }
+    if "f32key_f64band" in results:
+        line["band_vs_f64_speedup"] = round(results["f64"] / results["f32key_f64band"], 3)
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def _mode_available(coupe, pts, w, part):
+    try:
+        coupe.rcb_device(part[:1024], pts[:1024], w[:1024], 2, 0.05, mode="f32key_f64band")
+        return True
+    except coupe.CoupeError:
+        return False
+
+
+def _traffic_per_launch(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+if __name__ == "__main__":
+    sys.exit(main())

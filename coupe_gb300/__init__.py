@@ -37,6 +37,7 @@ EXPORTED = [
     "coupe_data_fn", "coupe_rcb", "coupe_rib",
     "coupe_gpu_rcb", "coupe_gpu_rib", "coupe_gpu_rcb_device", "coupe_gpu_rib_device",
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
+    "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
 ]
 
 
@@ -102,8 +103,34 @@ def lib():
     L.coupe_gpu_last_error.restype = ctypes.c_char_p
     L.coupe_gpu_version.argtypes = []
     L.coupe_gpu_version.restype = ctypes.c_char_p
+    L.coupe_gpu_profile.argtypes = [i32]
+    L.coupe_gpu_profile.restype = i32
+    L.coupe_gpu_profile_read.argtypes = [vp, vp, vp, i32]
+    L.coupe_gpu_profile_read.restype = i32
+    L.coupe_gpu_kernel_name.argtypes = [i32]
+    L.coupe_gpu_kernel_name.restype = ctypes.c_char_p
     _lib = L
     return L
+
+
+def profile(enable=True):
+    """Turns the per-launch CUDA-event profiler on or off (resets totals)."""
+    _check(lib().coupe_gpu_profile(1 if enable else 0))
+
+
+def profile_read():
+    """{kernel: {"launches", "bytes", "ms"}} accumulated since profile()."""
+    L = lib()
+    cap = 64
+    c = (ctypes.c_uint64 * cap)()
+    b = (ctypes.c_uint64 * cap)()
+    m = (ctypes.c_double * cap)()
+    k = L.coupe_gpu_profile_read(c, b, m, cap)
+    out = {}
+    for i in range(min(k, cap)):
+        if c[i]:
+            out[L.coupe_gpu_kernel_name(i).decode()] = {"launches": int(c[i]), "bytes": int(b[i]), "ms": float(m[i])}
+    return out
 
 
 def last_stats():

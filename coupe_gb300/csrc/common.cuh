@@ -285,6 +285,8 @@ struct RunScalars {
     uint64_t splits;
     uint32_t err;
     int32_t fscale;
+    uint32_t wide;  // nonzero: some weight is not an integer in [0, 2^20)
+    uint32_t pad;
 };
 
 }  // namespace cg

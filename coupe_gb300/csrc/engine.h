@@ -6,6 +6,7 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/coupe_gpu.h"
 
@@ -27,6 +28,35 @@ struct RunArgs {
     cudaStream_t stream = nullptr;
 };
 
+// Kernel kinds timed by the optional per-launch profiler.
+enum KernelId {
+    KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_SCAN, KID_CHILDREN, KID_REORDER,
+    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_COUNT
+};
+const char *kernel_name(int id);
+
+// Per-launch CUDA-event profiler: when on, every launch of a run is bracketed
+// by two events on its stream; after the run's final synchronisation the
+// elapsed times and the launch's algorithmic bytes are accumulated per kind.
+struct Profiler {
+    bool on = false;
+    struct Rec {
+        int id;
+        uint64_t bytes;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    uint64_t count[KID_COUNT] = {};
+    uint64_t bytes[KID_COUNT] = {};
+    double ms[KID_COUNT] = {};
+    cudaEvent_t take();
+    void begin(int id, uint64_t bytes, cudaStream_t s);
+    void end(cudaStream_t s);
+    void resolve();  // call after the stream synchronised
+    void reset();
+};
+
 // Per-device state: a stream, a grow-only workspace and pinned scalars.
 // Runs on one device are serialised by `mu`.
 struct DevCtx {
@@ -37,6 +67,7 @@ struct DevCtx {
     size_t ws_cap = 0;
     void *h_pinned = nullptr;  // pinned host scratch for scalar read-backs
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    Profiler prof;
     std::mutex mu;
 };
 

@@ -11,6 +11,68 @@
 
 namespace cg {
 
+const char *kernel_name(int id) {
+    static const char *names[KID_COUNT] = {"k_convert", "k_wabs_max", "k_wsum", "k_root", "k_hist", "k_decide",
+                                           "k_scan_list", "k_children", "k_reorder", "k_assign", "k_fill_u64",
+                                           "k_moments"};
+    return id >= 0 && id < KID_COUNT ? names[id] : "?";
+}
+
+cudaEvent_t Profiler::take() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+void Profiler::begin(int id, uint64_t nbytes, cudaStream_t s) {
+    if (!on) return;
+    Rec r;
+    r.id = id;
+    r.bytes = nbytes;
+    r.a = take();
+    r.b = take();
+    if (!r.a || !r.b) return;
+    cudaEventRecord(r.a, s);
+    recs.push_back(r);
+}
+
+void Profiler::end(cudaStream_t s) {
+    if (!on || recs.empty()) return;
+    cudaEventRecord(recs.back().b, s);
+}
+
+void Profiler::resolve() {
+    for (const Rec &r : recs) {
+        float ms_ = 0.f;
+        if (cudaEventElapsedTime(&ms_, r.a, r.b) == cudaSuccess) {
+            count[r.id] += 1;
+            bytes[r.id] += r.bytes;
+            ms[r.id] += ms_;
+        } else {
+            cudaGetLastError();
+        }
+        pool.push_back(r.a);
+        pool.push_back(r.b);
+    }
+    recs.clear();
+}
+
+void Profiler::reset() {
+    for (int i = 0; i < KID_COUNT; ++i) {
+        count[i] = 0;
+        bytes[i] = 0;
+        ms[i] = 0.0;
+    }
+}
+
 int cuda_fail(cudaError_t e, const char *what, std::string *err) {
     if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
     cudaGetLastError();  // clear a sticky launch error of this thread

@@ -355,4 +355,30 @@ const char *coupe_gpu_last_error(void) { return t_err.c_str(); }
 
 const char *coupe_gpu_version(void) { return "coupe-gpu 0.1.0 (sm_103a)"; }
 
+int coupe_gpu_profile(int enable) {
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) return COUPE_ERR_CRASH;
+    std::lock_guard<std::mutex> lock(C->mu);
+    C->prof.on = enable != 0;
+    C->prof.reset();
+    return COUPE_ERR_OK;
+}
+
+int coupe_gpu_profile_read(uint64_t *counts, uint64_t *bytes, double *ms, int capacity) {
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) return 0;
+    std::lock_guard<std::mutex> lock(C->mu);
+    int n = capacity < cg::KID_COUNT ? capacity : cg::KID_COUNT;
+    for (int i = 0; i < n; ++i) {
+        if (counts) counts[i] = C->prof.count[i];
+        if (bytes) bytes[i] = C->prof.bytes[i];
+        if (ms) ms[i] = C->prof.ms[i];
+    }
+    return cg::KID_COUNT;
+}
+
+const char *coupe_gpu_kernel_name(int id) { return cg::kernel_name(id); }
+
 }  // extern "C"

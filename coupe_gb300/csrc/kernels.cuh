@@ -32,6 +32,7 @@ constexpr uint64_t LB_AGG = 1ull << 62;      // look-back: aggregate published
 constexpr uint64_t LB_INCL = 2ull << 62;     // look-back: inclusive prefix published
 constexpr uint64_t LB_VALUE = (1ull << 62) - 1;
 constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
+constexpr int PACK_WBITS_IN = 20;            // packed histograms take weights below 2^20
 
 // ---------------------------------------------------------------------------
 // Small reductions
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                                                    typename KT::T *__restrict__ k1,
                                                    typename KT::T *__restrict__ k2, RunScalars *rs) {
     typedef typename KT::T K;
+    __shared__ uint64_t red[2 * 3][NWARPS];
     uint64_t mn[3], mx[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -156,10 +158,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         mx[d] = ord_f64(-1.7976931348623157e308);
     }
     K *outs[3] = {k0, k1, k2};
-    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
-        double p[D], q[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) p[d] = pts[i * D + d];
+    auto point = [&](const double *p, double *q) {
         if (M.on) {
 #pragma unroll
             for (int r = 0; r < D; ++r) {
@@ -173,23 +172,69 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             for (int d = 0; d < D; ++d) q[d] = p[d];
         }
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            outs[d][i] = KT::from_f64(q[d]);
+        for (int d = 0; d < D; ++d)
             if (q[d] == q[d]) {
-                uint64_t o = ord_f64(q[d]);
+                const uint64_t o = ord_f64(q[d]);
                 mn[d] = o < mn[d] ? o : mn[d];
                 mx[d] = o > mx[d] ? o : mx[d];
             }
+    };
+    const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x, stride = (uint64_t)gridDim.x * BLOCK;
+    // groups of 4 points: 16-byte loads of the AoS input, 16-byte key stores
+    const bool vec = ((uintptr_t)pts & 15) == 0;
+    const uint64_t groups = vec ? n / 4 : 0;
+    for (uint64_t g = tid; g < groups; g += stride) {
+        double flat[4 * D];
+        const double2 *src = (const double2 *)(pts + g * 4 * D);
+#pragma unroll
+        for (int v = 0; v < 2 * D; ++v) {
+            const double2 t = src[v];
+            flat[2 * v] = t.x;
+            flat[2 * v + 1] = t.y;
+        }
+        double q[4][D];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) point(flat + j * D, q[j]);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            if (sizeof(K) == 4) {
+                float4 o = make_float4((float)q[0][d], (float)q[1][d], (float)q[2][d], (float)q[3][d]);
+                *(float4 *)((float *)outs[d] + 4 * g) = o;
+            } else {
+                double2 *dst = (double2 *)((double *)outs[d] + 4 * g);
+                dst[0] = make_double2(q[0][d], q[1][d]);
+                dst[1] = make_double2(q[2][d], q[3][d]);
+            }
         }
     }
+    for (uint64_t i = groups * 4 + tid; i < n; i += stride) {
+        double q[D];
+        point(pts + i * D, q);
+#pragma unroll
+        for (int d = 0; d < D; ++d) outs[d][i] = KT::from_f64(q[d]);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-        uint64_t a = warp_min_u64(mn[d]);
-        uint64_t b = warp_max_u64(mx[d]);
-        if ((threadIdx.x & 31) == 0) {
-            atomicMin((unsigned long long *)&rs->bbox_min_ord[d], (unsigned long long)a);
-            atomicMax((unsigned long long *)&rs->bbox_max_ord[d], (unsigned long long)b);
+        const uint64_t a = warp_min_u64(mn[d]), b = warp_max_u64(mx[d]);
+        if (lane == 0) {
+            red[2 * d][warp] = a;
+            red[2 * d + 1][warp] = b;
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * D) {
+        const int d = threadIdx.x >> 1;
+        const bool is_max = threadIdx.x & 1;
+        uint64_t v = red[threadIdx.x][0];
+        for (int w = 1; w < NWARPS; ++w) {
+            const uint64_t u = red[threadIdx.x][w];
+            v = is_max ? (u > v ? u : v) : (u < v ? u : v);
+        }
+        if (is_max)
+            atomicMax((unsigned long long *)&rs->bbox_max_ord[d], (unsigned long long)v);
+        else
+            atomicMin((unsigned long long *)&rs->bbox_min_ord[d], (unsigned long long)v);
     }
 }
 
@@ -215,17 +260,21 @@ __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict
     uint64_t acc[WT::LIMBS];
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) acc[l] = 0;
+    bool wide = WT::LIMBS > 1;
     for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        const typename WT::S wi = w[i];
         uint64_t q[WT::LIMBS];
-        WT::limbs(w[i], fs, q);
+        WT::limbs(wi, fs, q);
 #pragma unroll
         for (int l = 0; l < WT::LIMBS; ++l) acc[l] += q[l];
+        if (WT::LIMBS == 1) wide |= !(wi >= 0 && wi < (1 << PACK_WBITS_IN));
     }
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) {
         uint64_t v = warp_sum_u64(acc[l]);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long *)&rs->wsum_limbs[l], (unsigned long long)v);
     }
+    if (__any_sync(0xffffffffu, wide) && (threadIdx.x & 31) == 0) atomicOr(&rs->wide, 1u);
 }
 
 // Root segment of level 0 (rcb_recurse's first call, recursive_bisection.rs:696).
@@ -262,17 +311,23 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
 }
 
 // ---------------------------------------------------------------------------
-// Candidate-cut tree of a segment: node i (heap order) holds the cut that
-// coupe's loop computes after the decisions spelled by i's path from the
-// root; leaves (bins) are in key order.
+// Candidate cuts of a segment.  The 2^nbk - 1 cuts that coupe's loop can
+// compute in its next nbk steps from the interval [lo, hi]
+// (recursive_bisection.rs:472, 564-571) form a binary tree whose in-order
+// sequence is non-decreasing: heap node (depth d, position p) has in-order
+// rank (2p+1) 2^(nbk-1-d) - 1.  A key's bin is the number of cuts c with
+// !(key < c), i.e. the leaf reached by descending the tree with
+// `key < c ? left : right`; bins are in key order.
 // ---------------------------------------------------------------------------
 template <class KT>
-__device__ __forceinline__ void build_cuts(typename KT::T lo, typename KT::T hi, int nbk, typename KT::T *cuts) {
+__device__ __forceinline__ void build_sorted_cuts(typename KT::T lo, typename KT::T hi, int nbk,
+                                                  typename KT::T *cuts) {
     typedef typename KT::T K;
     const int nodes = (1 << nbk) - 1;
     for (int i = threadIdx.x; i < nodes; i += blockDim.x) {
         const uint32_t id1 = (uint32_t)i + 1;  // 1-based heap id
         const int depth = 31 - __clz(id1);
+        const uint32_t p = id1 - (1u << depth);
         K a = lo, b = hi;
         for (int l = depth - 1; l >= 0; --l) {
             K c = KT::mid(a, b);
@@ -281,18 +336,51 @@ __device__ __forceinline__ void build_cuts(typename KT::T lo, typename KT::T hi,
             else
                 b = c;
         }
-        cuts[i] = KT::mid(a, b);
+        cuts[((2 * p + 1) << (nbk - 1 - depth)) - 1] = KT::mid(a, b);
     }
 }
 
+// Bin lookup: an arithmetic first guess (cuts are close to an even grid),
+// corrected against the exact sorted cuts; a binary search when the
+// interval is degenerate or not finite.
+struct BinGuess {
+    float lo, scale;
+    int fast;
+};
+
 template <class KT>
-__device__ __forceinline__ int bin_of(typename KT::T key, const typename KT::T *cuts, int nbk) {
-    int node = 0;
-    for (int l = 0; l < nbk; ++l) node = 2 * node + 1 + (key < cuts[node] ? 0 : 1);
-    return node - ((1 << nbk) - 1);
+__device__ __forceinline__ BinGuess bin_guess(typename KT::T lo, typename KT::T hi, int nb) {
+    BinGuess g;
+    const float l = (float)lo, h = (float)hi;
+    const float sc = (float)nb / (h - l);
+    g.lo = l;
+    g.scale = sc;
+    g.fast = (h > l) && isfinite(l) && isfinite(h) && isfinite(sc);
+    return g;
 }
 
-// Global histogram slots: [segment][bin]; bmin stores ~ord(key) so that an
+template <class KT>
+__device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT::T *cuts, int nb, const BinGuess &g) {
+    if (g.fast) {
+        float f = ((float)key - g.lo) * g.scale;
+        f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
+        int b = __float2int_rz(f);
+        while (b > 0 && key < cuts[b - 1]) --b;
+        while (b < nb - 1 && !(key < cuts[b])) ++b;
+        return b;
+    }
+    int l = 0, r = nb - 1;
+    while (l < r) {
+        const int m = (l + r) >> 1;
+        if (key < cuts[m])
+            r = m;
+        else
+            l = m + 1;
+    }
+    return l;
+}
+
+// Global histogram slots: [segment][bin]; inv stores ~ord(key) so that an
 // all-zero slot means "no key" and atomicMax of ~ord is a min of keys.
 template <class KT, class WT>
 struct Hist {
@@ -301,8 +389,17 @@ struct Hist {
     typename KT::Ord *inv;
 };
 
+// Packed shared-memory accumulator for integer weights in [0, 2^20): one
+// 64-bit atomic adds (1 << 44) + w, so count and weight share a word; a
+// window of fewer than 2^20 items can neither overflow the 20-bit count nor
+// carry out of the 44-bit weight sum.
+constexpr int PACK_SHIFT = 44;
+constexpr uint64_t PACK_WMASK = (1ull << PACK_SHIFT) - 1;
+constexpr uint64_t PACK_WINDOW = 1ull << 19;
+
 // ---------------------------------------------------------------------------
-// k_hist: one static chunk of the active items per CTA.
+// k_hist: one static chunk of the active items per CTA; per segment piece a
+// shared-memory histogram flushed to the segment's global bins.
 // ---------------------------------------------------------------------------
 template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
@@ -314,24 +411,27 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
     typedef typename KT::Ord O;
     constexpr int L = WT::LIMBS;
     __shared__ K cuts[MAX_NB];
+    __shared__ uint64_t sw[MAX_NB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
     __shared__ uint32_t scnt[MAX_NB];
-    __shared__ uint64_t sw[MAX_NB * L];
     __shared__ O sinv[MAX_NB];
     const int NB = 1 << nbk;
     const int fs = L > 1 ? rs->fscale : 0;
+    const bool packed = L == 1 && rs->wide == 0;
     const uint64_t T = P[nlist];
     const uint64_t c0 = T * blockIdx.x / gridDim.x, c1 = T * (blockIdx.x + 1) / gridDim.x;
     if (c0 >= c1) return;
     uint32_t k = upper_index(P, nlist + 1, c0);
     uint64_t pos = c0;
+    int cur_s = -1;
     while (pos < c1) {
         const uint32_t s = list[k];
-        const uint64_t pe = min(c1, P[k + 1]);
+        const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
         const Seg<KT> &sg = segs[s];
         const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
         const K lo = sg.lo, hi = sg.hi;
         __syncthreads();
-        build_cuts<KT>(lo, hi, nbk, cuts);
+        if ((int)s != cur_s) build_sorted_cuts<KT>(lo, hi, nbk, cuts);
+        cur_s = (int)s;
         for (int i = threadIdx.x; i < NB; i += BLOCK) {
             scnt[i] = 0;
             sinv[i] = 0;
@@ -339,6 +439,15 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
             for (int l = 0; l < L; ++l) sw[i * L + l] = 0;
         }
         __syncthreads();
+        const BinGuess g = bin_guess<KT>(lo, hi, NB);
+        // Keys below lo are all in bin 0 and keys >= hi all in bin NB-1 (every
+        // cut lies in [lo, hi]).  Once the interval has narrowed, most keys are
+        // there, so they are summed in registers instead of by atomics.
+        uint32_t out_c[2] = {0, 0};
+        uint64_t out_w[2][L];
+        O out_inv[2] = {0, 0};
+#pragma unroll
+        for (int l = 0; l < L; ++l) out_w[0][l] = out_w[1][l] = 0;
         for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HIST_ITEMS) {
             K kv[HIST_ITEMS];
             typename WT::S wv[HIST_ITEMS];
@@ -354,30 +463,75 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
             for (int i = 0; i < HIST_ITEMS; ++i) {
                 const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
                 if (e < b && kv[i] == kv[i]) {
-                    const int bin = bin_of<KT>(kv[i], cuts, nbk);
-                    atomicAdd(&scnt[bin], 1u);
                     uint64_t q[L];
                     WT::limbs(wv[i], fs, q);
+                    const int side = kv[i] < lo ? 0 : (!(kv[i] < hi) ? 1 : -1);
+                    if (side >= 0) {
+                        out_c[side] += 1;
+#pragma unroll
+                        for (int l = 0; l < L; ++l) out_w[side][l] += q[l];
+                        const O v = (O)~KT::ord(kv[i]);
+                        out_inv[side] = v > out_inv[side] ? v : out_inv[side];
+                        continue;
+                    }
+                    const int bin = bin_sorted<KT>(kv[i], cuts, NB, g);
+                    if (packed) {
+                        atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+                    } else {
+                        atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
+                    }
+                    const O v = (O)~KT::ord(kv[i]);
+                    if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+                }
+            }
+        }
+        // fold the out-of-interval sums into the edge bins (one lane per warp)
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const uint64_t c = warp_sum_u64(out_c[side]);
+            uint64_t wsum[L];
+#pragma unroll
+            for (int l = 0; l < L; ++l) wsum[l] = warp_sum_u64(out_w[side][l]);
+            const O inv = (O)~warp_min_ord<O>((O)~out_inv[side]);
+            if ((threadIdx.x & 31) == 0 && c) {
+                const int bin = side == 0 ? 0 : NB - 1;
+                if (packed) {
+                    atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((c << PACK_SHIFT) | wsum[0]));
+                } else {
+                    atomicAdd(&scnt[bin], (uint32_t)c);
 #pragma unroll
                     for (int l = 0; l < L; ++l)
-                        if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
-                    atomic_max_ord(&sinv[bin], (O)~KT::ord(kv[i]));
+                        if (wsum[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)wsum[l]);
                 }
+                atomic_max_ord(&sinv[bin], inv);
             }
         }
         __syncthreads();
         for (int i = threadIdx.x; i < NB; i += BLOCK) {
-            if (scnt[i]) {
-                const size_t g = (size_t)s * NB + i;
-                atomicAdd(&H.cnt[g], scnt[i]);
+            uint32_t c;
+            uint64_t wl[L];
+            if (packed) {
+                c = (uint32_t)(sw[i] >> PACK_SHIFT);
+                wl[0] = sw[i] & PACK_WMASK;
+            } else {
+                c = scnt[i];
+#pragma unroll
+                for (int l = 0; l < L; ++l) wl[l] = sw[i * L + l];
+            }
+            if (c) {
+                const size_t gi = (size_t)s * NB + i;
+                atomicAdd(&H.cnt[gi], c);
 #pragma unroll
                 for (int l = 0; l < L; ++l)
-                    if (sw[i * L + l]) atomicAdd((unsigned long long *)&H.w[g * L + l], (unsigned long long)sw[i * L + l]);
-                atomic_max_ord(&H.inv[g], sinv[i]);
+                    if (wl[l]) atomicAdd((unsigned long long *)&H.w[gi * L + l], (unsigned long long)wl[l]);
+                atomic_max_ord(&H.inv[gi], sinv[i]);
             }
         }
         pos = pe;
-        ++k;
+        if (pos == P[k + 1]) ++k;
     }
 }
 
@@ -673,6 +827,11 @@ struct ReorderArgs {
     RunScalars *rs;
 };
 
+template <int D, class KT, class WT>
+constexpr size_t reorder_smem() {
+    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + sizeof(uint32_t));
+}
+
 template <class KT>
 __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg) {
     return sg.state == SEG_ALLLEFT || key < sg.pivot;
@@ -694,7 +853,12 @@ __device__ __forceinline__ void stage_out(const T *stage, T *dst, uint32_t tcoun
 template <int D, class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
-    __shared__ uint64_t stage_raw[R_TILE];
+    typedef typename WT::S WS;
+    // staging: D key tiles, a weight tile and an index tile (dynamic smem)
+    extern __shared__ __align__(16) unsigned char dsm[];
+    K *stK = (K *)dsm;
+    WS *stW = (WS *)(dsm + (size_t)D * R_TILE * sizeof(K));
+    uint32_t *stI = (uint32_t *)(dsm + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS));
     __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
     __shared__ uint64_t sh[33];
     __shared__ uint64_t s_ticket, s_prefix;
@@ -761,14 +925,27 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
             const uint64_t seg_end = sg.off + sg.n, left_end = sg.off + sg.nleft;
             for (uint64_t ts = pa; ts < pb; ts += R_TILE) {
                 const uint32_t tcount = (uint32_t)min((uint64_t)R_TILE, pb - ts);
+                // all loads of the tile first: one memory round trip per tile
+                K kv[D][R_ITEMS];
+                WS wv[R_ITEMS];
+                uint32_t iv[R_ITEMS];
+#pragma unroll
+                for (int i = 0; i < R_ITEMS; ++i) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    if (li < tcount) {
+#pragma unroll
+                        for (int d = 0; d < D; ++d) kv[d][i] = A.ksrc[d][ts + li];
+                        wv[i] = A.wsrc[ts + li];
+                        iv[i] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
+                    }
+                }
                 bool fl[R_ITEMS];
                 uint32_t bal[R_ITEMS];
 #pragma unroll
                 for (int i = 0; i < R_ITEMS; ++i) {
                     const uint32_t li = i * BLOCK + threadIdx.x;
-                    const bool valid = li < tcount;
-                    const K key = valid ? kc[ts + li] : (K)0;
-                    fl[i] = valid && goes_left<KT>(key, sg);
+                    const K key = A.coord == 0 ? kv[0][i] : (A.coord == 1 ? kv[1][i] : kv[D - 1][i]);
+                    fl[i] = li < tcount && goes_left<KT>(key, sg);
                     bal[i] = __ballot_sync(0xffffffffu, fl[i]);
                     if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
                 }
@@ -800,51 +977,28 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
                 }
                 __syncthreads();
                 const uint32_t tile_left = (uint32_t)sh[0];
-                uint16_t pos[R_ITEMS];
 #pragma unroll
                 for (int i = 0; i < R_ITEMS; ++i) {
                     const uint32_t li = i * BLOCK + threadIdx.x;
-                    const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & ((1u << lane) - 1));
-                    pos[i] = (uint16_t)(fl[i] ? before : tile_left + (li - before));
+                    if (li < tcount) {
+                        const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & ((1u << lane) - 1));
+                        const uint32_t p = fl[i] ? before : tile_left + (li - before);
+#pragma unroll
+                        for (int d = 0; d < D; ++d) stK[d * R_TILE + p] = kv[d][i];
+                        stW[p] = wv[i];
+                        stI[p] = iv[i];
+                    }
                 }
+                __syncthreads();
                 const uint64_t left_base = sg.off + running;
                 const uint64_t right_base = sg.off + sg.nleft + (ts - sg.off - running);
-                // keys
 #pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    K *st = (K *)stage_raw;
-#pragma unroll
-                    for (int i = 0; i < R_ITEMS; ++i) {
-                        const uint32_t li = i * BLOCK + threadIdx.x;
-                        if (li < tcount) st[pos[i]] = A.ksrc[d][ts + li];
-                    }
-                    __syncthreads();
-                    stage_out<K>(st, A.kdst[d], tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
-                    __syncthreads();
-                }
-                {
-                    typedef typename WT::S WS;
-                    WS *st = (WS *)stage_raw;
-#pragma unroll
-                    for (int i = 0; i < R_ITEMS; ++i) {
-                        const uint32_t li = i * BLOCK + threadIdx.x;
-                        if (li < tcount) st[pos[i]] = A.wsrc[ts + li];
-                    }
-                    __syncthreads();
-                    stage_out<WS>(st, A.wdst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
-                    __syncthreads();
-                }
-                {
-                    uint32_t *st = (uint32_t *)stage_raw;
-#pragma unroll
-                    for (int i = 0; i < R_ITEMS; ++i) {
-                        const uint32_t li = i * BLOCK + threadIdx.x;
-                        if (li < tcount) st[pos[i]] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
-                    }
-                    __syncthreads();
-                    stage_out<uint32_t>(st, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
-                    __syncthreads();
-                }
+                for (int d = 0; d < D; ++d)
+                    stage_out<K>(stK + d * R_TILE, A.kdst[d], tcount, tile_left, left_base, right_base, seg_end, left_end,
+                                 A.rs);
+                stage_out<WS>(stW, A.wdst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                stage_out<uint32_t>(stI, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                __syncthreads();
                 running += tile_left;
             }
         }

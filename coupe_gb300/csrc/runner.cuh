@@ -20,11 +20,15 @@ namespace cg {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call, err);  \
     } while (0)
 
-#define CG_LAUNCHED()                                             \
-    do {                                                          \
-        cudaError_t e_ = cudaGetLastError();                      \
+// Launches a kernel, bracketed by profiler events when profiling is on.
+#define CG_LAUNCH(kid, nbytes, ...)                                 \
+    do {                                                            \
+        C.prof.begin((kid), (nbytes), s);                           \
+        __VA_ARGS__;                                                \
+        cudaError_t e_ = cudaGetLastError();                        \
         if (e_ != cudaSuccess) return cuda_fail(e_, "launch", err); \
-        ++st->kernel_launches;                                    \
+        C.prof.end(s);                                              \
+        ++st->kernel_launches;                                      \
     } while (0)
 
 struct Bump {
@@ -98,8 +102,9 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     }
     if (a.iter_count == 0) {
         // rcb_recurse with iter_count == 0 stores id 0 everywhere (:589-602)
-        k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part, n, 0);
-        CG_LAUNCHED();
+        CG_LAUNCH(KID_FILL, n * 8,
+                  k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part,
+                                                                                                            n, 0));
         CG_CK(cudaStreamSynchronize(s));
         return COUPE_ERR_OK;
     }
@@ -107,7 +112,10 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     uint64_t scap = a.iter_count >= 40 ? n : std::min<uint64_t>(n, 1ull << a.iter_count);
     scap = std::max<uint64_t>(scap, 1);
     const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
-    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, 0);
+    constexpr size_t r_smem = reorder_smem<D, KT, WT>();
+    CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)r_smem));
+    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
     uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * 4 - 1) / ((uint64_t)g_reorder * 4));
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
     const uint64_t nchunks = (n + chunk - 1) / chunk;
@@ -139,20 +147,18 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     std::memset(&M, 0, sizeof(M));
     M.on = a.has_matrix ? 1 : 0;
     for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
-    k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2], B.rs);
-    CG_LAUNCHED();
+    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
+    CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
+              k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
+                                                          B.rs));
     const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
     if (WT::LIMBS > 1) {
-        k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs);
-        CG_LAUNCHED();
+        CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs));
     }
-    k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs);
-    CG_LAUNCHED();
-    k_root<KT, WT><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs);
-    CG_LAUNCHED();
+    CG_LAUNCH(KID_WSUM, n * sw, k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs));
+    CG_LAUNCH(KID_ROOT, 0, k_root<KT, WT><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
 
     // algorithmic bytes: the input read and the SoA keys written
-    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
     uint64_t bytes = n * (D * 8 + sw) + n * D * sk + n * sw;  // convert + weight sum
     if (WT::LIMBS > 1) bytes += n * sw;
 
@@ -175,25 +181,28 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         Seg<KT> *segs = B.segs[cur];
         int li = 0;  // list / P buffer in use
         uint64_t nlist = S;
-        k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk, n, B.rs);
-        CG_LAUNCHED();
+        CG_LAUNCH(KID_HIST, n * (sk + sw),
+                  k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
+                                                          n, B.rs));
         ++st->hist_passes;
         st->hist_points += n;
         bytes += n * (sk + sw);
         for (;;) {
-            k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(segs, B.list[li], (uint32_t)nlist, H,
-                                                                                      nbk, a.tolerance, B.flags, B.rs);
-            CG_LAUNCHED();
-            k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1], B.P[li ^ 1], B.rs);
-            CG_LAUNCHED();
+            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WT::LIMBS + sizeof(typename KT::Ord)),
+                      k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
+                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs));
+            CG_LAUNCH(KID_SCAN, 0,
+                      k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
+                                                         B.P[li ^ 1], B.rs));
             CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
             CG_CK(cudaStreamSynchronize(s));
             if (h_rs->err) break;
             if (h_rs->nactive == 0) break;
             li ^= 1;
             nlist = h_rs->nactive;
-            k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk, n, B.rs);
-            CG_LAUNCHED();
+            CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
+                      k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
+                                                              nbk, n, B.rs));
             ++st->hist_passes;
             st->hist_points += h_rs->total_active;
             bytes += h_rs->total_active * (sk + sw);
@@ -201,12 +210,12 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         if (h_rs->err) break;
         const bool last = L + 1 == a.iter_count;
         const int nxt = cur ^ 1;
-        k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[nxt], B.list[0], B.P[0], n,
-                                             B.rs);
-        CG_LAUNCHED();
+        CG_LAUNCH(KID_CHILDREN, 0,
+                  k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[nxt],
+                                                        B.list[0], B.P[0], n, B.rs));
         if (last) {
-            k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs);
-            CG_LAUNCHED();
+            CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
+                      k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs));
             bytes += n * (sk + (ic ? 4 : 0) + 8);
             st->levels = L + 1;
             break;
@@ -234,8 +243,8 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         R.idst = B.idx[nxt];
         R.lb = B.lb;
         R.rs = B.rs;
-        k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, 0, s>>>(R);
-        CG_LAUNCHED();
+        CG_LAUNCH(KID_REORDER, 2 * n * (D * sk + sw + 4) - (ic ? 0 : n * 4),
+                  k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
         bytes += n * sk /* flag pre-count */ + 2 * n * (D * sk + sw + 4) - (ic ? 0 : n * 4);
         cur = nxt;
         w_user = false;
@@ -245,6 +254,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     CG_CK(cudaEventRecord(C.ev1, s));
     CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
     CG_CK(cudaStreamSynchronize(s));
+    C.prof.resolve();
     float ms = 0.f;
     cudaEventElapsedTime(&ms, C.ev0, C.ev1);
     st->device_ms = ms;

@@ -88,6 +88,19 @@ void coupe_gpu_last_stats(struct coupe_gpu_stats *out);
 /* Detailed message of the calling thread's last error ("" if none). */
 const char *coupe_gpu_last_error(void);
 
+/* Per-launch profiler of the calling device: enable != 0 turns it on, 0
+ * off; both reset the totals.  When on, every kernel launch is bracketed by
+ * CUDA events on its stream (small overhead). */
+int coupe_gpu_profile(int enable);
+
+/* Copies per-kernel totals since the last coupe_gpu_profile call: launches,
+ * algorithmic bytes and milliseconds, for up to `capacity` kernel kinds.
+ * Returns the number of kinds. */
+int coupe_gpu_profile_read(uint64_t *counts, uint64_t *bytes, double *ms, int capacity);
+
+/* Name of kernel kind `id` (as reported by coupe_gpu_profile_read). */
+const char *coupe_gpu_kernel_name(int id);
+
 /* Library version string. */
 const char *coupe_gpu_version(void);
 

@@ -14,6 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PATH = os.path.join(HERE, "build", "liboracle_rcb.so")
 
 REF32, F64 = 0, 1
+NAN_RIGHT = 0x100  # mode flag: NaN keys always go right (the GPU rule)
 FSUM_SEQ, FSUM_FIXED = 0, 1
 _WT = {np.dtype(np.int32): 0, np.dtype(np.int64): 1, np.dtype(np.float64): 2}
 

@@ -52,6 +52,10 @@ enum { OR_INT = 0, OR_INT64 = 1, OR_DOUBLE = 2 };
 // Key precision: REF32 restates the reference (f32 keys and cuts); F64 is the
 // same algorithm with every f32 replaced by f64.
 enum { OR_REF32 = 0, OR_F64 = 1 };
+// Mode flag: partition on `key < pivot` with NaN keys always on the right
+// (the GPU engine's rule) instead of coupe's Hoare scans, which leave a
+// NaN-keyed item on either side depending on its position in the segment.
+enum { OR_NAN_RIGHT = 0x100 };
 // How f64 weights are summed: sequentially left to right, or in the 128-bit
 // fixed-point scheme (order independent, see fixed_q / fixed_to_f64).
 enum { OR_FSUM_SEQ = 0, OR_FSUM_FIXED = 1 };
@@ -222,6 +226,7 @@ struct Ctx {
     int fscale;
     bool parallel;
     size_t min_len;  // rayon with_min_len(4096)
+    bool nan_right;
     uint64_t *part;
     oracle_stats st;
 };
@@ -253,6 +258,33 @@ static size_t reorder_split(Items<K, WT> &it, int dim, size_t pivot, int coord) 
     }
     swap_items(it, dim, 0, l);
     return l;
+}
+
+// Stable two-way partition on `key < pivot value` (NaN keys go right).
+template <class K, class WT>
+static size_t stable_split(Items<K, WT> &it, int dim, size_t pivot, int coord) {
+    const K pv = it.keys[coord][pivot];
+    std::vector<size_t> order;
+    order.reserve(it.n);
+    for (size_t i = 0; i < it.n; ++i)
+        if (it.keys[coord][i] < pv) order.push_back(i);
+    const size_t nl = order.size();
+    for (size_t i = 0; i < it.n; ++i)
+        if (!(it.keys[coord][i] < pv)) order.push_back(i);
+    for (int d = 0; d < dim; ++d) {
+        std::vector<K> tmp(it.n);
+        for (size_t i = 0; i < it.n; ++i) tmp[i] = it.keys[d][order[i]];
+        std::copy(tmp.begin(), tmp.end(), it.keys[d]);
+    }
+    std::vector<typename WT::S> tw(it.n);
+    std::vector<uint64_t> ti(it.n);
+    for (size_t i = 0; i < it.n; ++i) {
+        tw[i] = it.w[order[i]];
+        ti[i] = it.idx[order[i]];
+    }
+    std::copy(tw.begin(), tw.end(), it.w);
+    std::copy(ti.begin(), ti.end(), it.idx);
+    return nl;
 }
 
 template <class K, class WT>
@@ -369,7 +401,8 @@ static SplitOut<K, WT> split(Ctx &cx, Items<K, WT> &it, int coord, K mn, K mx, t
                 }
                 if (!(it.keys[coord][a.nidx] == kmin)) cx.st.pivot_ties += 1;
             }
-            o.nleft = reorder_split(it, cx.dim, a.nidx, coord);
+            o.nleft = cx.nan_right ? stable_split(it, cx.dim, a.nidx, coord)
+                                   : reorder_split(it, cx.dim, a.nidx, coord);
             o.wl = wl;
             o.split_pos = t;
             break;
@@ -547,6 +580,8 @@ static int rcb_entry(uint64_t *part, size_t n, int dim, const double *pts, int w
     cx.tol = tol;
     cx.min_len = 4096;
     cx.parallel = threads != 1;
+    cx.nan_right = (mode & OR_NAN_RIGHT) != 0;
+    mode &= 0xff;
     int rc = 0;
     if (!cx.parallel) {
         rc = mode == OR_F64 ? rcb_dispatch<double>(cx, part, n, pts, wtype, w, iter_count, fsum)

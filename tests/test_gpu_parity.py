@@ -116,3 +116,153 @@ def test_config1_uniform2d(coupe, oracle_mod):
     want, _ = oracle_mod.rcb(pts, w, cfg["iter_count"], cfg["tolerance"], threads=0)
     got = _gpu(coupe, pts, w, cfg["iter_count"], cfg["tolerance"])
     assert (want == got).all()
+
+
+# ---------------------------------------------------------------------------
+# Harder inputs: clusters, planes of equal keys, special values, weights that
+# take the general (non-packed) accumulation, integer wrap-around.
+# ---------------------------------------------------------------------------
+def _check(coupe, oracle_mod, pts, w, iters, tol, mode="ref32", fsum=None, nan_right=False):
+    om = _oracle_mode(mode) | (oracle_mod.NAN_RIGHT if nan_right else 0)
+    want, st = oracle_mod.rcb(pts, w, iters, tol, mode=om,
+                              fsum=oracle_mod.FSUM_FIXED if fsum is None else fsum)
+    got = _gpu(coupe, pts, w, iters, tol, mode=mode)
+    assert st["pivot_ties"] == 0
+    mism = int((want != got).sum())
+    assert mism == 0, "%d / %d ids differ" % (mism, len(pts))
+    return got, st
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f64"])
+def test_gaussian_clusters(coupe, oracle_mod, mode):
+    from coupe_gb300 import workloads
+    pts, w, cfg = workloads.gaussian_mixture3d(n=400_000, seed=3)
+    _check(coupe, oracle_mod, pts, w, cfg["iter_count"], cfg["tolerance"], mode)
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f64"])
+def test_planes_f64_weights(coupe, oracle_mod, mode):
+    from coupe_gb300 import workloads
+    pts, w, cfg = workloads.planes3d_lognormal(n=300_000, seed=4)
+    _check(coupe, oracle_mod, pts, w, 9, cfg["tolerance"], mode)
+
+
+def test_all_points_identical(coupe, oracle_mod):
+    pts = np.full((5000, 3), 1.25)
+    w = np.ones(5000, dtype=np.int64)
+    _check(coupe, oracle_mod, pts, w, 6, 0.05)
+
+
+def test_special_values(coupe, oracle_mod):
+    rng = np.random.default_rng(21)
+    pts = rng.standard_normal((20000, 2))
+    pts[::97, 0] = np.inf
+    pts[5::101, 1] = -np.inf
+    pts[7::89, 0] = np.nan
+    pts[::53, 1] = -0.0
+    pts[3::59, 0] = 1e300   # beyond f32: key becomes inf in REF32
+    pts[11::61, 1] = 1e-310  # subnormal f64
+    w = rng.integers(1, 5, size=len(pts), dtype=np.int64)
+    for mode in ("ref32", "f64"):
+        _check(coupe, oracle_mod, pts, w, 7, 0.02, mode)
+    # finite bounding box: signed zeros and subnormals
+    pts = rng.standard_normal((20000, 2))
+    pts[::53, 1] = -0.0
+    pts[::57, 1] = 0.0
+    pts[11::61, 1] = 1e-310
+    pts[13::67, 0] = -1e-40  # a subnormal f32 key
+    for mode in ("ref32", "f64"):
+        got, _ = _check(coupe, oracle_mod, pts, w, 7, 0.02, mode)
+        assert len(set(got.tolist())) > 64
+
+
+def test_nan_coordinates(coupe, oracle_mod):
+    """NaN keys: coupe's Hoare partition puts a NaN-keyed item left or right
+    depending on where it sits in the segment; the GPU sends it right.  Exact
+    against the oracle with that rule, and close to coupe's own placement."""
+    rng = np.random.default_rng(26)
+    pts = rng.standard_normal((20000, 2))
+    pts[7::89, 0] = np.nan
+    pts[3::97, 1] = np.nan
+    w = rng.integers(1, 5, size=len(pts), dtype=np.int64)
+    for mode in ("ref32", "f64"):
+        got, _ = _check(coupe, oracle_mod, pts, w, 7, 0.02, mode, nan_right=True)
+    ref, _ = oracle_mod.rcb(pts, w, 7, 0.02)
+    finite = np.isfinite(pts).all(axis=1)
+    assert (ref[finite] == got[finite]).mean() > 0.5
+
+
+def test_wide_negative_and_zero_weights(coupe, oracle_mod):
+    rng = np.random.default_rng(22)
+    pts = rng.random((60000, 3))
+    w = rng.integers(-(1 << 40), 1 << 40, size=len(pts), dtype=np.int64)
+    w[::7] = 0
+    _check(coupe, oracle_mod, pts, w, 8, 0.01)
+    w2 = np.zeros(len(pts), dtype=np.int64)  # sum 0: imbalance is NaN
+    _check(coupe, oracle_mod, pts, w2, 5, 0.01)
+
+
+def test_int32_wraparound(coupe, oracle_mod):
+    """c_int weights whose sums overflow 32 bits wrap like release-built Rust."""
+    rng = np.random.default_rng(23)
+    pts = rng.random((80000, 2))
+    w = rng.integers(1 << 28, (1 << 31) - 1, size=len(pts), dtype=np.int32)
+    _check(coupe, oracle_mod, pts, w, 6, 0.05)
+
+
+def test_f64_weights_wide_range(coupe, oracle_mod):
+    rng = np.random.default_rng(24)
+    pts = rng.random((50000, 3))
+    w = np.exp(rng.uniform(-30, 30, size=len(pts)))
+    w[::13] *= -1.0
+    for mode in ("ref32", "f64"):
+        _check(coupe, oracle_mod, pts, w, 7, 0.01, mode)
+
+
+def test_f64_weights_close_to_sequential_sums(coupe, oracle_mod):
+    """Against the oracle's sequential f64 sums (the reference's arithmetic up
+    to summation order): nearly all ids agree."""
+    rng = np.random.default_rng(25)
+    pts = rng.random((200000, 3))
+    w = rng.lognormal(0.0, 1.0, size=len(pts))
+    want, _ = oracle_mod.rcb(pts, w, 10, 0.01, fsum=oracle_mod.FSUM_SEQ)
+    got = _gpu(coupe, pts, w, 10, 0.01)
+    assert (want == got).mean() >= 0.9999
+
+
+def test_iter_count_zero(coupe):
+    pts = np.random.default_rng(1).random((1000, 2))
+    got = _gpu(coupe, pts, np.ones(1000, np.int64), 0, 0.05)
+    assert (got == 0).all()
+
+
+def test_rib_with_given_matrix(coupe, oracle_mod):
+    """Rib given the same basis change: bit-identical ids."""
+    torch = pytest.importorskip("torch")
+    from coupe_gb300 import workloads
+    pts, w, _ = workloads.hex_mesh_rib(side=48, seed=5)
+    M = oracle_mod.rib_matrix(pts)
+    want, _ = oracle_mod.rib(pts, w, 8, 0.01, matrix=M)
+    d_pts = torch.from_numpy(pts).cuda()
+    d_w = torch.from_numpy(w).cuda()
+    part = torch.empty(len(pts), dtype=torch.int64, device="cuda")
+    coupe.rcb_device(part, d_pts, d_w, 8, 0.01, matrix=M)
+    got = part.cpu().numpy().view(np.uint64)
+    assert (want == got).all()
+
+
+def test_rib_matrix_matches_oracle(coupe, oracle_mod):
+    torch = pytest.importorskip("torch")
+    from coupe_gb300 import workloads
+    pts, _, _ = workloads.hex_mesh_rib(side=40, seed=6)
+    M_o = oracle_mod.rib_matrix(pts)
+    M_g = coupe.rib_matrix_device(torch.from_numpy(pts).cuda())
+    assert np.allclose(M_g, M_o, rtol=1e-9, atol=1e-12)
+
+
+def test_rib_end_to_end(coupe, oracle_mod):
+    from coupe_gb300 import workloads
+    pts, w, _ = workloads.hex_mesh_rib(side=40, seed=7)
+    want, _ = oracle_mod.rib(pts, w, 8, 0.01)
+    got = _gpu(coupe, pts, w, 8, 0.01, rib=True)
+    assert (want == got).mean() >= 0.9999
