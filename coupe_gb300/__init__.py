@@ -38,6 +38,7 @@ EXPORTED = [
     "coupe_gpu_rcb", "coupe_gpu_rib", "coupe_gpu_rcb_device", "coupe_gpu_rib_device",
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
+    "coupe_gpu_set_option", "coupe_gpu_get_option",
 ]
 
 
@@ -109,8 +110,21 @@ def lib():
     L.coupe_gpu_profile_read.restype = i32
     L.coupe_gpu_kernel_name.argtypes = [i32]
     L.coupe_gpu_kernel_name.restype = ctypes.c_char_p
+    L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
+    L.coupe_gpu_set_option.restype = i32
+    L.coupe_gpu_get_option.argtypes = [ctypes.c_char_p]
+    L.coupe_gpu_get_option.restype = ctypes.c_int64
     _lib = L
     return L
+
+
+def set_option(name, value):
+    """Sets a scheduling knob (see include/coupe_gpu.h); never changes results."""
+    _check(lib().coupe_gpu_set_option(name.encode(), int(value)))
+
+
+def get_option(name):
+    return int(lib().coupe_gpu_get_option(name.encode()))
 
 
 def profile(enable=True):

@@ -261,6 +261,24 @@ struct Seg {
     K bmin[3], bmax[3];
 };
 
+// One finished split as the final traversal needs it: items with
+// (flags & TRAV_ALLLEFT) or key < pivot went to the left child.  `next` is
+// the index of the first child in the next level's segment list, or on the
+// last level the split segment's heap id.
+enum : uint32_t { TRAV_ALLLEFT = 1u, TRAV_HAS_LEFT = 2u };
+
+template <class KT>
+struct Trav {
+    typename KT::T pivot;
+    uint32_t flags;
+    uint64_t next;
+};
+
+constexpr int MAX_TRAV_LEVELS = 63;
+struct LevelOffsets {
+    uint64_t off[MAX_TRAV_LEVELS];
+};
+
 // Error bits raised by kernels (read by the host after each synchronisation).
 enum : uint32_t {
     ERR_LOOKBACK_TIMEOUT = 1u,

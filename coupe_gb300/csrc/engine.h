@@ -28,6 +28,19 @@ struct RunArgs {
     cudaStream_t stream = nullptr;
 };
 
+// Process-wide tuning knobs (coupe_gpu_set_option).  They change how the
+// work is scheduled, never the result.
+struct Tuning {
+    int force_index_path = 0;        // 1: carry input indices through every reorder
+    int max_nbk = 8;                 // bisection steps per histogram pass (2^max_nbk bins)
+    int reorder_chunks_per_cta = 4;  // reorder chunks per resident CTA
+};
+Tuning &tuning();
+
+// Largest number of recorded splits for which part ids come from a
+// traversal (k_traverse) rather than from indices carried through reorders.
+constexpr uint64_t TRAV_MAX_ENTRIES = 1ull << 22;
+
 // Kernel kinds timed by the optional per-launch profiler.
 enum KernelId {
     KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_SCAN, KID_CHILDREN, KID_REORDER,

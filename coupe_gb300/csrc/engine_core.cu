@@ -11,6 +11,11 @@
 
 namespace cg {
 
+Tuning &tuning() {
+    static Tuning t;
+    return t;
+}
+
 const char *kernel_name(int id) {
     static const char *names[KID_COUNT] = {"k_convert", "k_wabs_max", "k_wsum", "k_root", "k_hist", "k_decide",
                                            "k_scan_list", "k_children", "k_reorder", "k_assign", "k_fill_u64",

@@ -381,4 +381,25 @@ int coupe_gpu_profile_read(uint64_t *counts, uint64_t *bytes, double *ms, int ca
 
 const char *coupe_gpu_kernel_name(int id) { return cg::kernel_name(id); }
 
+static int *option_slot(const char *name) {
+    if (!name) return nullptr;
+    cg::Tuning &t = cg::tuning();
+    if (!std::strcmp(name, "force_index_path")) return &t.force_index_path;
+    if (!std::strcmp(name, "max_nbk")) return &t.max_nbk;
+    if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
+    return nullptr;
+}
+
+int coupe_gpu_set_option(const char *name, int64_t value) {
+    int *p = option_slot(name);
+    if (!p) return COUPE_ERR_BAD_TYPE;
+    *p = (int)value;
+    return COUPE_ERR_OK;
+}
+
+int64_t coupe_gpu_get_option(const char *name) {
+    int *p = option_slot(name);
+    return p ? *p : -1;
+}
+
 }  // extern "C"

@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ 
 template <class KT, class WT>
 __global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ segs, uint32_t S, int coord, int D,
                                                    int write, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
-                                                   uint64_t n_total, RunScalars *rs) {
+                                                   uint64_t n_total, Trav<KT> *trav, RunScalars *rs) {
     typedef typename KT::T K;
     __shared__ uint64_t sh[33];
     uint64_t outc = 0;
@@ -758,6 +758,13 @@ __global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ s
             const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
             if (nl > 0) hmin = hl < hmin ? hl : hmin;
             if (nr > 0) hmin = hr < hmin ? hr : hmin;
+            if (trav) {
+                Trav<KT> t;
+                t.pivot = sg.pivot;
+                t.flags = (sg.state == SEG_ALLLEFT ? TRAV_ALLLEFT : 0u) | (nl > 0 ? TRAV_HAS_LEFT : 0u);
+                t.next = write ? outc + ci : sg.heap;
+                trav[s] = t;
+            }
             if (write) {
                 uint64_t c = outc + ci;
                 const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
@@ -936,7 +943,7 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
 #pragma unroll
                         for (int d = 0; d < D; ++d) kv[d][i] = A.ksrc[d][ts + li];
                         wv[i] = A.wsrc[ts + li];
-                        iv[i] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
+                        if (A.idst) iv[i] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
                     }
                 }
                 bool fl[R_ITEMS];
@@ -986,7 +993,7 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
 #pragma unroll
                         for (int d = 0; d < D; ++d) stK[d * R_TILE + p] = kv[d][i];
                         stW[p] = wv[i];
-                        stI[p] = iv[i];
+                        if (A.idst) stI[p] = iv[i];
                     }
                 }
                 __syncthreads();
@@ -997,11 +1004,57 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
                     stage_out<K>(stK + d * R_TILE, A.kdst[d], tcount, tile_left, left_base, right_base, seg_end, left_end,
                                  A.rs);
                 stage_out<WS>(stW, A.wdst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
-                stage_out<uint32_t>(stI, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
+                if (A.idst)
+                    stage_out<uint32_t>(stI, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end,
+                                        A.rs);
                 __syncthreads();
                 running += tile_left;
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_traverse: part ids in input order without carrying item indices through
+// the reorders: each item walks the recorded splits from the root with its
+// own keys (the copy of the level-0 keys), taking the side the reorder gave
+// it, and gets its leaf's heap id minus the smallest heap id
+// (recursive_bisection.rs:589-601, 698-702).  Coalesced reads and writes.
+// ---------------------------------------------------------------------------
+constexpr int TRAV_SMEM_BYTES = 40 * 1024;
+
+template <int D, class KT>
+__global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__ trav, uint64_t trav_total,
+                                                    LevelOffsets lv, int levels, const typename KT::T *__restrict__ k0,
+                                                    const typename KT::T *__restrict__ k1,
+                                                    const typename KT::T *__restrict__ k2, uint64_t n,
+                                                    uint64_t *__restrict__ part, const RunScalars *rs) {
+    typedef typename KT::T K;
+    constexpr int CAP = TRAV_SMEM_BYTES / sizeof(Trav<KT>);
+    __shared__ Trav<KT> st[CAP];
+    const uint64_t cached = trav_total < (uint64_t)CAP ? trav_total : (uint64_t)CAP;
+    for (uint64_t j = threadIdx.x; j < cached; j += BLOCK) st[j] = trav[j];
+    __syncthreads();
+    const uint64_t hmin = rs->min_heap;
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        K key[3];
+        key[0] = k0[i];
+        key[1] = k1[i];
+        if (D == 3) key[2] = k2[i];
+        uint64_t seg = 0, id = 0;
+        int c = 0;
+        for (int L = 0; L < levels; ++L) {
+            const uint64_t j = lv.off[L] + seg;
+            const Trav<KT> t = j < cached ? st[j] : trav[j];
+            const K kc = c == 0 ? key[0] : (c == 1 ? key[1] : key[D - 1]);
+            const bool left = (t.flags & TRAV_ALLLEFT) || kc < t.pivot;
+            if (L + 1 < levels)
+                seg = t.next + (left ? 0 : ((t.flags & TRAV_HAS_LEFT) ? 1 : 0));
+            else
+                id = (left ? 2 * t.next + 1 : 2 * t.next + 2) - hmin;
+            c = c + 1 == D ? 0 : c + 1;
+        }
+        part[i] = id;
     }
 }
 

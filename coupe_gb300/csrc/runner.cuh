@@ -47,9 +47,9 @@ template <int D, class KT, class WT>
 struct Buffers {
     typedef typename KT::T K;
     typedef typename KT::Ord O;
-    K *keys[2][3];
+    K *keys[3][3];  // [0]: level-0 keys in input order (kept); [1], [2]: reorder ping-pong
     typename WT::S *w[2];
-    uint32_t *idx[2];
+    uint32_t *idx[2];  // input index of each item (index path only)
     Seg<KT> *segs[2];
     uint32_t *list[2];
     uint64_t *P[2];
@@ -58,15 +58,16 @@ struct Buffers {
     uint64_t *hw;
     O *hinv;
     uint64_t *lb;
+    Trav<KT> *trav;  // finished splits of every level (traversal path only)
     RunScalars *rs;
     uint64_t hist_bins;
-    uint64_t lb_cap;
 
-    size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap) {
+    size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap, bool index_path, uint64_t tcap) {
+        for (int k = 0; k < 3; ++k)
+            for (int d = 0; d < 3; ++d) keys[k][d] = d < D ? b.take<K>(n) : nullptr;
         for (int s = 0; s < 2; ++s) {
-            for (int d = 0; d < 3; ++d) keys[s][d] = d < D ? b.take<K>(n) : nullptr;
             w[s] = b.take<typename WT::S>(n);
-            idx[s] = b.take<uint32_t>(n);
+            idx[s] = index_path ? b.take<uint32_t>(n) : nullptr;
             segs[s] = b.take<Seg<KT>>(scap);
             list[s] = b.take<uint32_t>(scap);
             P[s] = b.take<uint64_t>(scap + 1);
@@ -76,9 +77,9 @@ struct Buffers {
         hw = b.take<uint64_t>(hb * WT::LIMBS);
         hinv = b.take<O>(hb);
         lb = b.take<uint64_t>(lbcap);
+        trav = index_path ? nullptr : b.take<Trav<KT>>(tcap);
         rs = b.take<RunScalars>(1);
         hist_bins = hb;
-        lb_cap = lbcap;
         return b.off;
     }
 };
@@ -92,6 +93,7 @@ static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem
 template <int D, class KT, class WT>
 int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
     typedef typename KT::T K;
+    const Tuning &tu = tuning();
     const uint64_t n = a.n;
     cudaStream_t s = a.stream ? a.stream : C.stream;
     st->points = n;
@@ -108,25 +110,32 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         CG_CK(cudaStreamSynchronize(s));
         return COUPE_ERR_OK;
     }
+    const uint64_t iters = a.iter_count;
     // segment capacity: a level holds at most min(2^level, n) segments
-    uint64_t scap = a.iter_count >= 40 ? n : std::min<uint64_t>(n, 1ull << a.iter_count);
+    uint64_t scap = iters >= 40 ? n : std::min<uint64_t>(n, 1ull << iters);
     scap = std::max<uint64_t>(scap, 1);
     const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
+    // Part ids come from a traversal of the recorded splits unless the tree is
+    // too large to record; then every reorder carries the input indices.
+    uint64_t tcap = 0;
+    for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
+    const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
     constexpr size_t r_smem = reorder_smem<D, KT, WT>();
     CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)r_smem));
     const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
-    uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * 4 - 1) / ((uint64_t)g_reorder * 4));
+    const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
+    uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
     const uint64_t nchunks = (n + chunk - 1) / chunk;
 
     Buffers<D, KT, WT> B;
     Bump dry{nullptr, 0};
-    const size_t need = B.carve(dry, n, scap, hb, nchunks);
+    const size_t need = B.carve(dry, n, scap, hb, nchunks, index_path, tcap);
     int rc = ensure_workspace(C, need, err);
     if (rc != COUPE_ERR_OK) return rc;
     Bump real{(char *)C.ws, 0};
-    B.carve(real, n, scap, hb, nchunks);
+    B.carve(real, n, scap, hb, nchunks, index_path, tcap);
     RunScalars *h_rs = (RunScalars *)C.h_pinned;
 
     const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
@@ -147,7 +156,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     std::memset(&M, 0, sizeof(M));
     M.on = a.has_matrix ? 1 : 0;
     for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
-    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
+    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S), si = index_path ? 4 : 0;
     CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
               k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
                                                           B.rs));
@@ -162,23 +171,26 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     uint64_t bytes = n * (D * 8 + sw) + n * D * sk + n * sw;  // convert + weight sum
     if (WT::LIMBS > 1) bytes += n * sw;
 
-    int cur = 0;       // buffers of the current level
-    bool w_user = true;  // level 0 reads the caller's weights and implicit indices
+    int kb = 0;          // key buffer of the current level
+    int sb = 0;          // segment table / weight buffer of the current level
+    bool level0 = true;  // level 0 reads the caller's weights and implicit indices
     uint64_t S = 1;
-    for (uint64_t L = 0; L < a.iter_count; ++L) {
+    LevelOffsets lv;
+    uint64_t trav_used = 0;
+    for (uint64_t L = 0; L < iters; ++L) {
         const int coord = (int)(L % D);
         // bins per segment: as many bisection steps per pass as the budget allows
-        int nbk = MAX_NBK;
+        int nbk = std::min(MAX_NBK, std::max(1, tu.max_nbk));
         while (nbk > 1 && S * (1ull << nbk) > B.hist_bins) --nbk;
         const uint64_t NB = 1ull << nbk;
         Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
         CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
         CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
-        const K *kc = B.keys[cur][coord];
-        const typename WT::S *wc = w_user ? w_in : B.w[cur];
-        const uint32_t *ic = w_user ? nullptr : B.idx[cur];
-        Seg<KT> *segs = B.segs[cur];
+        const K *kc = B.keys[kb][coord];
+        const typename WT::S *wc = level0 ? w_in : B.w[sb];
+        const uint32_t *ic = level0 ? nullptr : B.idx[sb];
+        Seg<KT> *segs = B.segs[sb];
         int li = 0;  // list / P buffer in use
         uint64_t nlist = S;
         CG_LAUNCH(KID_HIST, n * (sk + sw),
@@ -208,15 +220,28 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
             bytes += h_rs->total_active * (sk + sw);
         }
         if (h_rs->err) break;
-        const bool last = L + 1 == a.iter_count;
-        const int nxt = cur ^ 1;
+        const bool last = L + 1 == iters;
+        const int snext = sb ^ 1;
+        Trav<KT> *trav_l = nullptr;
+        if (!index_path) {
+            lv.off[L] = trav_used;
+            trav_l = B.trav + trav_used;
+            trav_used += S;
+        }
         CG_LAUNCH(KID_CHILDREN, 0,
-                  k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[nxt],
-                                                        B.list[0], B.P[0], n, B.rs));
+                  k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
+                                                        B.list[0], B.P[0], n, trav_l, B.rs));
         if (last) {
-            CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
-                      k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs));
-            bytes += n * (sk + (ic ? 4 : 0) + 8);
+            if (index_path) {
+                CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
+                          k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs));
+                bytes += n * (sk + (ic ? 4 : 0) + 8);
+            } else {
+                CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                          k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters, B.keys[0][0],
+                                                                       B.keys[0][1], B.keys[0][2], n, a.d_part, B.rs));
+                bytes += n * (D * sk + 8);
+            }
             st->levels = L + 1;
             break;
         }
@@ -226,6 +251,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         const uint64_t S_next = h_rs->nsegs_next;
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
+        const int kb_next = kb == 1 ? 2 : 1;
         ReorderArgs<D, KT, WT> R;
         R.segs = segs;
         R.S = (uint32_t)S;
@@ -234,20 +260,22 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         R.nchunks = nchunks;
         R.coord = coord;
         for (int d = 0; d < 3; ++d) {
-            R.ksrc[d] = B.keys[cur][d];
-            R.kdst[d] = B.keys[nxt][d];
+            R.ksrc[d] = B.keys[kb][d];
+            R.kdst[d] = B.keys[kb_next][d];
         }
         R.wsrc = wc;
-        R.wdst = B.w[nxt];
+        R.wdst = B.w[snext];
         R.isrc = ic;
-        R.idst = B.idx[nxt];
+        R.idst = index_path ? B.idx[snext] : nullptr;
         R.lb = B.lb;
         R.rs = B.rs;
-        CG_LAUNCH(KID_REORDER, 2 * n * (D * sk + sw + 4) - (ic ? 0 : n * 4),
+        const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
+        CG_LAUNCH(KID_REORDER, rbytes,
                   k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
-        bytes += n * sk /* flag pre-count */ + 2 * n * (D * sk + sw + 4) - (ic ? 0 : n * 4);
-        cur = nxt;
-        w_user = false;
+        bytes += n * sk /* flag pre-count */ + rbytes;
+        kb = kb_next;
+        sb = snext;
+        level0 = false;
         S = S_next;
         st->levels = L + 1;
     }

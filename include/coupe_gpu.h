@@ -101,6 +101,17 @@ int coupe_gpu_profile_read(uint64_t *counts, uint64_t *bytes, double *ms, int ca
 /* Name of kernel kind `id` (as reported by coupe_gpu_profile_read). */
 const char *coupe_gpu_kernel_name(int id);
 
+/* Process-wide scheduling knobs; none of them changes a result.
+ *   "force_index_path"        1: carry each point's input index through every
+ *                             reorder instead of tracing the recorded splits
+ *   "max_nbk"                 bisection steps per histogram pass (1..8)
+ *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
+ * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
+int coupe_gpu_set_option(const char *name, int64_t value);
+
+/* Current value of a knob, or -1 for an unknown name. */
+int64_t coupe_gpu_get_option(const char *name);
+
 /* Library version string. */
 const char *coupe_gpu_version(void);
 

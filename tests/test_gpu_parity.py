@@ -266,3 +266,28 @@ def test_rib_end_to_end(coupe, oracle_mod):
     want, _ = oracle_mod.rib(pts, w, 8, 0.01)
     got = _gpu(coupe, pts, w, 8, 0.01, rib=True)
     assert (want == got).mean() >= 0.9999
+
+
+@pytest.mark.parametrize("knobs", [{"force_index_path": 1}, {"max_nbk": 3}, {"max_nbk": 1},
+                                   {"reorder_chunks_per_cta": 1}, {"reorder_chunks_per_cta": 64}])
+def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
+    """Part ids through the index path, fewer bisection steps per pass and
+    other chunkings equal the oracle's."""
+    from coupe_gb300 import workloads
+    pts, w, cfg = workloads.gaussian_mixture3d(n=120_000, seed=9)
+    want, _ = oracle_mod.rcb(pts, w, 9, 0.01)
+    old = {k: coupe.get_option(k) for k in knobs}
+    try:
+        for k, v in knobs.items():
+            coupe.set_option(k, v)
+        for mode, om in (("ref32", 0), ("f64", 1)):
+            want, _ = oracle_mod.rcb(pts, w, 9, 0.01, mode=om)
+            got = _gpu(coupe, pts, w, 9, 0.01, mode=mode)
+            assert (want == got).all()
+        # deep tree on the same path
+        p2, w2 = _make(3000, 2, "i64", 11)
+        want2, _ = oracle_mod.rcb(p2, w2, 14, 0.05)
+        assert (want2 == _gpu(coupe, p2, w2, 14, 0.05)).all()
+    finally:
+        for k, v in old.items():
+            coupe.set_option(k, v)
