@@ -255,6 +255,8 @@ struct Seg {
     uint32_t nleft;  // result: items sent left
     uint32_t state;  // SEG_*
     uint32_t steps;  // bisection steps taken so far
+    uint32_t child;  // index of the first non-empty child in the next level
+    uint32_t pad;
     K lo, hi;        // current search interval on this level's axis
     K pivot;         // result: items with key < pivot go left
     K split_pos;     // result: the cut position

@@ -23,7 +23,7 @@ namespace cg {
 
 constexpr int BLOCK = 256;
 constexpr int NWARPS = BLOCK / 32;
-constexpr int MAX_NBK = 8;
+constexpr int MAX_NBK = 10;
 constexpr int MAX_NB = 1 << MAX_NBK;
 constexpr int HIST_ITEMS = 16;               // items per thread per hist iteration
 constexpr int R_ITEMS = 8;                   // items per thread per reorder tile
@@ -294,6 +294,8 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
     s.nleft = 0;
     s.state = SEG_ACTIVE;
     s.steps = 0;
+    s.child = 0;
+    s.pad = 0;
     for (int d = 0; d < 3; ++d) {
         double a = d < D ? unord_f64(rs->bbox_min_ord[d]) : 0.0;
         double b = d < D ? unord_f64(rs->bbox_max_ord[d]) : 0.0;
@@ -397,6 +399,13 @@ constexpr int PACK_SHIFT = 44;
 constexpr uint64_t PACK_WMASK = (1ull << PACK_SHIFT) - 1;
 constexpr uint64_t PACK_WINDOW = 1ull << 19;
 
+// Most bins per segment a histogram pass keeps in shared memory: four
+// 64-bit limbs per bin for f64 weights allow fewer.
+template <class WT>
+__host__ __device__ constexpr int hist_max_nbk() {
+    return WT::LIMBS > 1 ? 9 : MAX_NBK;
+}
+
 // ---------------------------------------------------------------------------
 // k_hist: one static chunk of the active items per CTA; per segment piece a
 // shared-memory histogram flushed to the segment's global bins.
@@ -410,10 +419,11 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
     typedef typename KT::T K;
     typedef typename KT::Ord O;
     constexpr int L = WT::LIMBS;
-    __shared__ K cuts[MAX_NB];
-    __shared__ uint64_t sw[MAX_NB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
-    __shared__ uint32_t scnt[MAX_NB];
-    __shared__ O sinv[MAX_NB];
+    constexpr int HNB = 1 << hist_max_nbk<WT>();
+    __shared__ K cuts[HNB];
+    __shared__ uint64_t sw[HNB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
+    __shared__ uint32_t scnt[HNB];
+    __shared__ O sinv[HNB];
     const int NB = 1 << nbk;
     const int fs = L > 1 ? rs->fscale : 0;
     const bool packed = L == 1 && rs->wide == 0;
@@ -465,13 +475,21 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
                 if (e < b && kv[i] == kv[i]) {
                     uint64_t q[L];
                     WT::limbs(wv[i], fs, q);
-                    const int side = kv[i] < lo ? 0 : (!(kv[i] < hi) ? 1 : -1);
-                    if (side >= 0) {
-                        out_c[side] += 1;
-#pragma unroll
-                        for (int l = 0; l < L; ++l) out_w[side][l] += q[l];
+                    const bool below = kv[i] < lo, above = !below && !(kv[i] < hi);
+                    if (below || above) {
+                        // constant indices only: keeps the sums in registers
                         const O v = (O)~KT::ord(kv[i]);
-                        out_inv[side] = v > out_inv[side] ? v : out_inv[side];
+                        if (below) {
+                            out_c[0] += 1;
+#pragma unroll
+                            for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
+                            out_inv[0] = v > out_inv[0] ? v : out_inv[0];
+                        } else {
+                            out_c[1] += 1;
+#pragma unroll
+                            for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
+                            out_inv[1] = v > out_inv[1] ? v : out_inv[1];
+                        }
                         continue;
                     }
                     const int bin = bin_sorted<KT>(kv[i], cuts, NB, g);
@@ -554,24 +572,42 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     const uint32_t s = list[k];
     Seg<KT> sg = segs[s];
     const int NB = 1 << nbk;
-    const int per = NB >= 32 ? NB / 32 : 1;
+    // Lane l owns the block of BS consecutive bins starting at l*BS.  Steps
+    // whose halves span whole blocks use the block totals; once a half is
+    // narrower than a block, the one block left is spread over the lanes.
+    const int BS = NB >= 32 ? NB / 32 : 1;
     const int fs = L > 1 ? rs->fscale : 0;
-    // owned bins: [lane*per, lane*per + per)
-    uint32_t bc[MAX_NB / 32];
-    uint64_t bw[MAX_NB / 32][L];
-    O bm[MAX_NB / 32];
+    const size_t g0 = (size_t)s * NB;
+    auto load_bin = [&](int b, uint64_t &c, uint64_t *w, O &m) {
+        const size_t g = g0 + b;
+        c = H.cnt[g];
 #pragma unroll
-    for (int j = 0; j < MAX_NB / 32; ++j) {
-        const int b = lane * per + j;
-        const bool own = j < per && b < NB;
-        const size_t g = (size_t)s * NB + b;
-        bc[j] = own ? H.cnt[g] : 0;
+        for (int l = 0; l < L; ++l) w[l] = H.w[g * L + l];
+        const O o = (O)~H.inv[g];
+        m = o > KT::ORD_INF ? KT::ORD_INF : o;
+    };
+    uint64_t Tc = 0, Tw[L];
+    O Tm = KT::ORD_INF;
 #pragma unroll
-        for (int l = 0; l < L; ++l) bw[j][l] = own ? H.w[g * L + l] : 0;
-        O inv = own ? H.inv[g] : (O)0;
-        O o = (O)~inv;
-        bm[j] = o > KT::ORD_INF ? KT::ORD_INF : o;
+    for (int l = 0; l < L; ++l) Tw[l] = 0;
+    if (lane * BS < NB) {
+        for (int j = 0; j < BS; ++j) {
+            uint64_t c, w[L];
+            O m;
+            load_bin(lane * BS + j, c, w, m);
+            Tc += c;
+#pragma unroll
+            for (int l = 0; l < L; ++l) Tw[l] += w[l];
+            Tm = m < Tm ? m : Tm;
+        }
     }
+    bool fine = false;
+    int fine_base = 0;
+    uint64_t Fc = 0, Fw[L];
+    O Fm = KT::ORD_INF;
+#pragma unroll
+    for (int l = 0; l < L; ++l) Fw[l] = 0;
+
     const V sum = WT::from_bits(sg.sum);
     K lo = sg.lo, hi = sg.hi;
     uint64_t prev = sg.prev;
@@ -588,23 +624,24 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     uint64_t nleft = 0;
     for (int step = 0; step < nbk; ++step) {
         const int mid_b = (lo_b + hi_b) >> 1;
-        uint64_t c = 0;
-        uint64_t wp[L];
-#pragma unroll
-        for (int l = 0; l < L; ++l) wp[l] = 0;
+        if (!fine && mid_b - lo_b < BS) {
+            fine = true;
+            fine_base = lo_b - lo_b % BS;  // the block holding [lo_b, hi_b)
+            if (lane < BS) load_bin(fine_base + lane, Fc, Fw, Fm);
+        }
+        // this lane's unit: a whole block (coarse) or one bin (fine)
+        const int u0 = fine ? fine_base + lane : lane * BS;
+        const bool has = fine ? lane < BS : u0 < NB;
+        uint64_t c = 0, wp[L];
         O m = KT::ORD_INF;
 #pragma unroll
-        for (int j = 0; j < MAX_NB / 32; ++j) {
-            const int b = lane * per + j;
-            if (j < per && b < NB) {
-                if (b >= lo_b && b < mid_b) {
-                    c += bc[j];
+        for (int l = 0; l < L; ++l) wp[l] = 0;
+        if (has && u0 >= lo_b && u0 < mid_b) {
+            c = fine ? Fc : Tc;
 #pragma unroll
-                    for (int l = 0; l < L; ++l) wp[l] += bw[j][l];
-                }
-                if (b >= mid_b && b < hi_b) m = bm[j] < m ? bm[j] : m;
-            }
+            for (int l = 0; l < L; ++l) wp[l] = fine ? Fw[l] : Tw[l];
         }
+        if (has && u0 >= mid_b && u0 < hi_b) m = fine ? Fm : Tm;
         c = warp_sum_u64(c);
 #pragma unroll
         for (int l = 0; l < L; ++l) wp[l] = warp_sum_u64(wp[l]);
@@ -677,16 +714,12 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         }
     } else {
         // keep searching: clear this segment's bins for the next pass
+        for (int b = lane; b < NB; b += 32) {
+            const size_t g = g0 + b;
+            H.cnt[g] = 0;
 #pragma unroll
-        for (int j = 0; j < MAX_NB / 32; ++j) {
-            const int b = lane * per + j;
-            if (j < per && b < NB) {
-                const size_t g = (size_t)s * NB + b;
-                H.cnt[g] = 0;
-#pragma unroll
-                for (int l = 0; l < L; ++l) H.w[g * L + l] = 0;
-                H.inv[g] = 0;
-            }
+            for (int l = 0; l < L; ++l) H.w[g * L + l] = 0;
+            H.inv[g] = 0;
         }
         if (lane == 0) {
             Seg<KT> &o = segs[s];
@@ -735,7 +768,7 @@ __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ 
 // dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
 // the smallest heap id among the children (the id offset, :698-702).
 template <class KT, class WT>
-__global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ segs, uint32_t S, int coord, int D,
+__global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D,
                                                    int write, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
                                                    uint64_t n_total, Trav<KT> *trav, RunScalars *rs) {
     typedef typename KT::T K;
@@ -765,6 +798,7 @@ __global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ s
                 t.next = write ? outc + ci : sg.heap;
                 trav[s] = t;
             }
+            if (write) segs[s].child = (uint32_t)(outc + ci);
             if (write) {
                 uint64_t c = outc + ci;
                 const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
@@ -781,6 +815,8 @@ __global__ void __launch_bounds__(1024) k_children(const Seg<KT> *__restrict__ s
                     ch.nleft = 0;
                     ch.state = SEG_ACTIVE;
                     ch.steps = 0;
+                    ch.child = 0;
+                    ch.pad = 0;
                     for (int d = 0; d < 3; ++d) {
                         ch.bmin[d] = sg.bmin[d];
                         ch.bmax[d] = sg.bmax[d];
@@ -831,12 +867,23 @@ struct ReorderArgs {
     const uint32_t *isrc;  // NULL: identity
     uint32_t *idst;
     uint64_t *lb;  // look-back words, one per chunk, zeroed
+    // Fused first histogram pass of the next level: both children of a
+    // segment start their search on the same interval (the segment's box on
+    // the next axis), so each item is binned once into its side's bins.
+    Hist<KT, WT> hn;  // next level's bins (zeroed); hn.cnt == NULL: not fused
+    int nbk_next;
     RunScalars *rs;
 };
 
 template <int D, class KT, class WT>
-constexpr size_t reorder_smem() {
+__host__ __device__ constexpr size_t reorder_stage_smem() {
     return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + sizeof(uint32_t));
+}
+
+// Shared memory of the fused histogram for 2^nbk bins per side.
+template <class KT, class WT>
+__host__ __device__ constexpr size_t reorder_hist_smem(int nbk) {
+    return (size_t)(1 << nbk) * (sizeof(typename KT::T) + 2 * (8 * WT::LIMBS + 4 + sizeof(typename KT::Ord)));
 }
 
 template <class KT>
@@ -860,18 +907,30 @@ __device__ __forceinline__ void stage_out(const T *stage, T *dst, uint32_t tcoun
 template <int D, class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
+    typedef typename KT::Ord O;
     typedef typename WT::S WS;
+    constexpr int L = WT::LIMBS;
     // staging: D key tiles, a weight tile and an index tile (dynamic smem)
     extern __shared__ __align__(16) unsigned char dsm[];
     K *stK = (K *)dsm;
     WS *stW = (WS *)(dsm + (size_t)D * R_TILE * sizeof(K));
     uint32_t *stI = (uint32_t *)(dsm + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS));
+    // fused histogram (after the staging): per side 2^nbk_next bins
+    const bool fuse = A.hn.cnt != nullptr;
+    const int NBn = 1 << A.nbk_next;
+    uint64_t *hw = (uint64_t *)(dsm + reorder_stage_smem<D, KT, WT>());  // [2][NBn][L]
+    O *hinv = (O *)(hw + 2 * NBn * L);                                   // [2][NBn]
+    uint32_t *hcnt = (uint32_t *)(hinv + 2 * NBn);                       // [2][NBn]
+    K *cuts = (K *)(hcnt + 2 * NBn);                                     // [NBn - 1]
+    const bool packed = L == 1 && A.rs->wide == 0;
+    const int fs = L > 1 ? A.rs->fscale : 0;
+    const int nc = A.coord + 1 == D ? 0 : A.coord + 1;
     __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
     __shared__ uint64_t sh[33];
     __shared__ uint64_t s_ticket, s_prefix;
     __shared__ uint32_t s_fail;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const K *__restrict__ kc = A.ksrc[A.coord];
+    const K *__restrict__ kc = A.coord == 0 ? A.ksrc[0] : (A.coord == 1 ? A.ksrc[1] : A.ksrc[2]);
     for (;;) {
         if (threadIdx.x == 0) s_ticket = atomicAdd((unsigned long long *)&A.rs->ticket, 1ull);
         __syncthreads();
@@ -930,6 +989,23 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
             const uint64_t pa = max(c0, sg.off), pb = min(c1, sg.off + sg.n);
             uint64_t running = kk == kf ? prefix_first : 0;
             const uint64_t seg_end = sg.off + sg.n, left_end = sg.off + sg.nleft;
+            BinGuess g;
+            if (fuse) {
+                // the children's interval on the next axis (select, not index:
+                // a runtime index would move the segment record to local memory)
+                const K blo = nc == 0 ? sg.bmin[0] : (nc == 1 ? sg.bmin[1] : sg.bmin[2]);
+                const K bhi = nc == 0 ? sg.bmax[0] : (nc == 1 ? sg.bmax[1] : sg.bmax[2]);
+                __syncthreads();  // the previous piece's flush has read the bins
+                build_sorted_cuts<KT>(blo, bhi, A.nbk_next, cuts);
+                for (int i = threadIdx.x; i < 2 * NBn; i += BLOCK) {
+                    hcnt[i] = 0;
+                    hinv[i] = 0;
+#pragma unroll
+                    for (int l = 0; l < L; ++l) hw[i * L + l] = 0;
+                }
+                g = bin_guess<KT>(blo, bhi, NBn);
+                __syncthreads();
+            }
             for (uint64_t ts = pa; ts < pb; ts += R_TILE) {
                 const uint32_t tcount = (uint32_t)min((uint64_t)R_TILE, pb - ts);
                 // all loads of the tile first: one memory round trip per tile
@@ -955,6 +1031,29 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
                     fl[i] = li < tcount && goes_left<KT>(key, sg);
                     bal[i] = __ballot_sync(0xffffffffu, fl[i]);
                     if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
+                }
+                if (fuse) {
+#pragma unroll
+                    for (int i = 0; i < R_ITEMS; ++i) {
+                        const uint32_t li = i * BLOCK + threadIdx.x;
+                        const K key = nc == 0 ? kv[0][i] : (nc == 1 ? kv[1][i] : kv[D - 1][i]);
+                        if (li < tcount && key == key) {
+                            const int side = fl[i] ? 0 : 1;
+                            const int bin = side * NBn + bin_sorted<KT>(key, cuts, NBn, g);
+                            uint64_t q[L];
+                            WT::limbs(wv[i], fs, q);
+                            if (packed) {
+                                atomicAdd((unsigned long long *)&hw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+                            } else {
+                                atomicAdd(&hcnt[bin], 1u);
+#pragma unroll
+                                for (int l = 0; l < L; ++l)
+                                    if (q[l]) atomicAdd((unsigned long long *)&hw[bin * L + l], (unsigned long long)q[l]);
+                            }
+                            const O v = (O)~KT::ord(key);
+                            if (v > hinv[bin]) atomic_max_ord(&hinv[bin], v);
+                        }
+                    }
                 }
                 __syncthreads();
                 if (warp == 0) {
@@ -1009,6 +1108,31 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
                                         A.rs);
                 __syncthreads();
                 running += tile_left;
+            }
+            if (fuse) {
+                // flush this piece's bins into the two children's bins
+                for (int i = threadIdx.x; i < 2 * NBn; i += BLOCK) {
+                    const int side = i >= NBn;
+                    uint32_t c;
+                    uint64_t wl[L];
+                    if (packed) {
+                        c = (uint32_t)(hw[i] >> PACK_SHIFT);
+                        wl[0] = hw[i] & PACK_WMASK;
+                    } else {
+                        c = hcnt[i];
+#pragma unroll
+                        for (int l = 0; l < L; ++l) wl[l] = hw[i * L + l];
+                    }
+                    if (c) {
+                        const uint64_t child = sg.child + (side && sg.nleft > 0 ? 1 : 0);
+                        const size_t gi = (size_t)child * NBn + (i - side * NBn);
+                        atomicAdd(&A.hn.cnt[gi], c);
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            if (wl[l]) atomicAdd((unsigned long long *)&A.hn.w[gi * L + l], (unsigned long long)wl[l]);
+                        atomic_max_ord(&A.hn.inv[gi], hinv[i]);
+                    }
+                }
             }
         }
     }

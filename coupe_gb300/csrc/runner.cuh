@@ -120,12 +120,15 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     uint64_t tcap = 0;
     for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
     const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
-    constexpr size_t r_smem = reorder_smem<D, KT, WT>();
+    const int nbk_max = std::min(hist_max_nbk<WT>(), std::max(1, tu.max_nbk));
+    constexpr size_t r_stage = reorder_stage_smem<D, KT, WT>();
+    const size_t r_smem_max = r_stage + reorder_hist_smem<KT, WT>(nbk_max);
     CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)r_smem));
-    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
+                               (int)r_smem_max));
+    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem_max);
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
     uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
+    chunk = std::min<uint64_t>(chunk, PACK_WINDOW);  // a fused piece must fit a packed window
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
     const uint64_t nchunks = (n + chunk - 1) / chunk;
 
@@ -177,28 +180,35 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     uint64_t S = 1;
     LevelOffsets lv;
     uint64_t trav_used = 0;
+    // bins per segment: as many bisection steps per pass as the budget allows
+    auto pick_nbk = [&](uint64_t nseg) {
+        int k = nbk_max;
+        while (k > 1 && nseg * (1ull << k) > B.hist_bins) --k;
+        return k;
+    };
+    int nbk = pick_nbk(1);
+    bool bins_ready = false;  // this level's first pass was fused into the last reorder
+    Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
     for (uint64_t L = 0; L < iters; ++L) {
         const int coord = (int)(L % D);
-        // bins per segment: as many bisection steps per pass as the budget allows
-        int nbk = std::min(MAX_NBK, std::max(1, tu.max_nbk));
-        while (nbk > 1 && S * (1ull << nbk) > B.hist_bins) --nbk;
         const uint64_t NB = 1ull << nbk;
-        Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
-        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
-        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
-        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
         const K *kc = B.keys[kb][coord];
         const typename WT::S *wc = level0 ? w_in : B.w[sb];
         const uint32_t *ic = level0 ? nullptr : B.idx[sb];
         Seg<KT> *segs = B.segs[sb];
         int li = 0;  // list / P buffer in use
         uint64_t nlist = S;
-        CG_LAUNCH(KID_HIST, n * (sk + sw),
-                  k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
-                                                          n, B.rs));
-        ++st->hist_passes;
-        st->hist_points += n;
-        bytes += n * (sk + sw);
+        if (!bins_ready) {
+            CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
+            CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
+            CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
+            CG_LAUNCH(KID_HIST, n * (sk + sw),
+                      k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
+                                                              nbk, n, B.rs));
+            ++st->hist_passes;
+            st->hist_points += n;
+            bytes += n * (sk + sw);
+        }
         for (;;) {
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WT::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
@@ -249,6 +259,16 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         CG_CK(cudaStreamSynchronize(s));
         if (h_rs->err) break;
         const uint64_t S_next = h_rs->nsegs_next;
+        const int nbk_next = pick_nbk(S_next);
+        // fuse the next level's first histogram pass into this reorder unless
+        // its segments are so small that per-segment set-up would dominate
+        const bool fuse = tu.fuse_hist && n >= S_next * (uint64_t)tu.fuse_min_points;
+        if (fuse) {
+            const uint64_t NBn = 1ull << nbk_next;
+            CG_CK(cudaMemsetAsync(B.hcnt, 0, S_next * NBn * sizeof(uint32_t), s));
+            CG_CK(cudaMemsetAsync(B.hw, 0, S_next * NBn * WT::LIMBS * sizeof(uint64_t), s));
+            CG_CK(cudaMemsetAsync(B.hinv, 0, S_next * NBn * sizeof(typename KT::Ord), s));
+        }
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
         const int kb_next = kb == 1 ? 2 : 1;
@@ -268,15 +288,24 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         R.isrc = ic;
         R.idst = index_path ? B.idx[snext] : nullptr;
         R.lb = B.lb;
+        R.hn = fuse ? H : Hist<KT, WT>{nullptr, nullptr, nullptr};
+        R.nbk_next = nbk_next;
         R.rs = B.rs;
+        const size_t r_smem = r_stage + (fuse ? reorder_hist_smem<KT, WT>(nbk_next) : 0);
         const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
         CG_LAUNCH(KID_REORDER, rbytes,
                   k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
         bytes += n * sk /* flag pre-count */ + rbytes;
+        if (fuse) {
+            ++st->hist_passes;
+            st->hist_points += n;
+        }
         kb = kb_next;
         sb = snext;
         level0 = false;
         S = S_next;
+        nbk = nbk_next;
+        bins_ready = fuse;
         st->levels = L + 1;
     }
     CG_CK(cudaEventRecord(C.ev1, s));

@@ -268,8 +268,9 @@ def test_rib_end_to_end(coupe, oracle_mod):
     assert (want == got).mean() >= 0.9999
 
 
-@pytest.mark.parametrize("knobs", [{"force_index_path": 1}, {"max_nbk": 3}, {"max_nbk": 1},
-                                   {"reorder_chunks_per_cta": 1}, {"reorder_chunks_per_cta": 64}])
+@pytest.mark.parametrize("knobs", [{"force_index_path": 1}, {"max_nbk": 3}, {"max_nbk": 1}, {"max_nbk": 8},
+                                   {"reorder_chunks_per_cta": 4}, {"reorder_chunks_per_cta": 64},
+                                   {"fuse_hist": 0}, {"fuse_min_points": 1}, {"fuse_min_points": 1, "max_nbk": 5}])
 def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     """Part ids through the index path, fewer bisection steps per pass and
     other chunkings equal the oracle's."""
