@@ -38,7 +38,7 @@ EXPORTED = [
     "coupe_gpu_rcb", "coupe_gpu_rib", "coupe_gpu_rcb_device", "coupe_gpu_rib_device",
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
-    "coupe_gpu_set_option", "coupe_gpu_get_option",
+    "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
 ]
 
 
@@ -110,6 +110,8 @@ def lib():
     L.coupe_gpu_profile_read.restype = i32
     L.coupe_gpu_kernel_name.argtypes = [i32]
     L.coupe_gpu_kernel_name.restype = ctypes.c_char_p
+    L.coupe_gpu_f64_to_f32.argtypes = [vp, vp, u64, vp]
+    L.coupe_gpu_f64_to_f32.restype = i32
     L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     L.coupe_gpu_set_option.restype = i32
     L.coupe_gpu_get_option.argtypes = [ctypes.c_char_p]

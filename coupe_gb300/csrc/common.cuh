@@ -57,29 +57,113 @@ CG_HD double unord_f64(uint64_t u) {
 }
 
 // ---------------------------------------------------------------------------
-// Key precision.  KeyF32 is coupe's arithmetic (f32 keys, `(min + max) / 2.0`
-// in f32, f32 distances); KeyF64 the same algorithm in f64.
+// f64 -> f32 round-to-nearest-even from the IEEE-754 binary64/binary32
+// definitions, in integer instructions only.  GB300 executes f64 instructions
+// (including the f64 -> f32 conversion) at a small fraction of its integer
+// rate, so per-point conversions are done this way.  NaN gives a quiet NaN.
+// ---------------------------------------------------------------------------
+CG_HD uint32_t f64bits_to_f32bits(uint64_t b) {
+    const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ff);
+    const uint64_t m = b & 0x000fffffffffffffull;
+    if (e == 0x7ff) return sign | (m ? 0x7fc00000u : 0x7f800000u);
+    if (e == 0) return sign;  // f64 subnormals are far below half the least f32 subnormal
+    const uint64_t M = m | (1ull << 52);  // value = M * 2^(e - 1075)
+    const int E = e - 896;                // biased f32 exponent
+    if (E >= 1) {
+        uint64_t r = M >> 29;
+        const uint64_t rem = M & ((1ull << 29) - 1), half = 1ull << 28;
+        if (rem > half || (rem == half && (r & 1))) ++r;
+        // r in [2^23, 2^24]; a carry to 2^24 bumps the exponent (also to inf)
+        const uint64_t bits = ((uint64_t)E << 23) + (r - (1ull << 23));
+        return bits >= 0x7f800000ull ? (sign | 0x7f800000u) : (sign | (uint32_t)bits);
+    }
+    // subnormal (or zero) f32: r = M * 2^(e - 926)
+    const int sh = 926 - e;  // >= 30
+    if (sh >= 64) return sign;
+    uint64_t r = M >> sh;
+    const uint64_t rem = M & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (r & 1))) ++r;
+    return sign | (uint32_t)r;  // r == 2^23 is the least normal, as encoded
+}
+
+CG_HD uint64_t f64_bits(double v) {
+#ifdef __CUDA_ARCH__
+    return (uint64_t)__double_as_longlong(v);
+#else
+    uint64_t b;
+    memcpy(&b, &v, 8);
+    return b;
+#endif
+}
+CG_HD float f32_from_bits(uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Key precision.  A key type has a stored form T, an arithmetic form A, and
+// the per-point operations lt (IEEE `<`), isnan and approx (a float near the
+// value, for bin guesses).  Arithmetic (cuts, distances) only happens per
+// segment, on A.
+//   KeyF32: coupe's arithmetic — f32 keys, `(min + max) / 2.0` in f32, f32
+//           distances (recursive_bisection.rs:472-553, 674-679).
+//   KeyF64: the same algorithm in f64.  Keys are stored in the order-
+//           preserving u64 encoding, so that per-point comparisons are
+//           integer comparisons; -0.0 is stored as +0.0 and every NaN as
+//           the largest code, which keeps IEEE `<` semantics.
 // ---------------------------------------------------------------------------
 struct KeyF32 {
     typedef float T;
+    typedef float A;
     typedef uint32_t Ord;
     static constexpr Ord ORD_INF = 0xff800000u;  // ord_f32(+inf)
     CG_HD static Ord ord(T k) { return ord_f32(k); }
     CG_HD static T unord(Ord u) { return unord_f32(u); }
     CG_HD static T from_f64(double v) { return (float)v; }
-    CG_HD static T inf() { return unord_f32(ORD_INF); }
+    CG_HD static T from_f64_bits(uint64_t b) { return f32_from_bits(f64bits_to_f32bits(b)); }
+    CG_HD static A val(T k) { return k; }
+    CG_HD static A inf() { return unord_f32(ORD_INF); }
+    CG_HD static bool lt(T a, T b) { return a < b; }
+    CG_HD static bool isnan(T k) { return !(k == k); }
+    CG_HD static float approx(T k) { return k; }
     // recursive_bisection.rs:472 — (min + max) / 2.0 in f32
     CG_HD static T mid(T a, T b) { return (a + b) / 2.0f; }
 };
 struct KeyF64 {
-    typedef double T;
+    typedef uint64_t T;
+    typedef double A;
     typedef uint64_t Ord;
-    static constexpr Ord ORD_INF = 0xfff0000000000000ull;  // ord_f64(+inf)
-    CG_HD static Ord ord(T k) { return ord_f64(k); }
-    CG_HD static T unord(Ord u) { return unord_f64(u); }
-    CG_HD static T from_f64(double v) { return v; }
-    CG_HD static T inf() { return unord_f64(ORD_INF); }
-    CG_HD static T mid(T a, T b) { return (a + b) / 2.0; }
+    static constexpr Ord ORD_INF = 0xfff0000000000000ull;  // code of +inf
+    static constexpr T NAN_CODE = ~0ull;
+    CG_HD static T enc_bits(uint64_t b) {
+        if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return NAN_CODE;
+        if (b == 0x8000000000000000ull) b = 0;  // -0.0 compares equal to +0.0
+        return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+    }
+    CG_HD static Ord ord(T k) { return k; }
+    CG_HD static T unord(Ord u) { return u; }
+    CG_HD static T from_f64(double v) { return enc_bits(f64_bits(v)); }
+    CG_HD static T from_f64_bits(uint64_t b) { return enc_bits(b); }
+    CG_HD static A val(T k) { return k > ORD_INF ? unord_f64(0xfff8000000000000ull) : unord_f64(k); }
+    CG_HD static A inf() { return unord_f64(ORD_INF); }
+    CG_HD static bool isnan(T k) { return k > ORD_INF; }
+    CG_HD static bool lt(T a, T b) { return a < b && b <= ORD_INF; }
+    CG_HD static float approx(T k) {
+        // a float near the value, by truncating the f64 fields (integers only)
+        const uint64_t b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+        const uint32_t s = (uint32_t)(b >> 32) & 0x80000000u;
+        const int e = (int)((b >> 52) & 0x7ff) - 896;
+        if (e <= 0) return f32_from_bits(s);
+        if (e >= 255) return f32_from_bits(s | 0x7f800000u);
+        return f32_from_bits(s | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
+    }
+    CG_HD static T mid(T a, T b) { return from_f64((val(a) + val(b)) / 2.0); }
 };
 
 // ---------------------------------------------------------------------------
@@ -104,12 +188,21 @@ CG_HD int fixed_scale_from_max(double amax, uint64_t n) {
     return 126 - e - ceil_log2_u64(n);
 }
 
+// q(w) from the binary64 fields (integer instructions only: it runs per item).
 CG_HD unsigned __int128 fixed_q_bits(double w, int s) {
-    if (w == 0.0) return 0;
-    int ex;
-    double f = frexp(fabs(w), &ex);
-    uint64_t m = (uint64_t)ldexp(f, 53);  // exact, 2^52 <= m < 2^53
-    int x = ex - 53 + s;
+    uint64_t bits;
+#ifdef __CUDA_ARCH__
+    bits = (uint64_t)__double_as_longlong(w);
+#else
+    memcpy(&bits, &w, 8);
+#endif
+    const int be = (int)((bits >> 52) & 0x7ff);
+    const uint64_t frac = bits & 0x000fffffffffffffull;
+    if (be == 0 && frac == 0) return 0;
+    // |w| 2^s = m 2^x with m < 2^53
+    const uint64_t m = be ? (frac | (1ull << 52)) : frac;
+    const int x = (be ? be - 1075 : -1074) + s;
+    const bool neg = (bits >> 63) != 0;
     unsigned __int128 q;
     if (x >= 0) {
         q = (unsigned __int128)m << x;
@@ -125,7 +218,7 @@ CG_HD unsigned __int128 fixed_q_bits(double w, int s) {
             q = qi;
         }
     }
-    return w < 0 ? (unsigned __int128)0 - q : q;
+    return neg ? (unsigned __int128)0 - q : q;
 }
 
 CG_HD int clz128(unsigned __int128 a) {

@@ -36,6 +36,7 @@ struct Tuning {
     int reorder_chunks_per_cta = 1;  // reorder chunks per resident CTA
     int fuse_hist = 1;               // 1: next level's first histogram pass inside the reorder
     int fuse_min_points = 4096;      // ... when its segments average at least this many points
+    int fuse_max_nbk = 9;            // bisection steps of a fused pass (its bins share the reorder's smem)
 };
 Tuning &tuning();
 
@@ -98,6 +99,9 @@ int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
 // The Rib basis change (obb_to_aabb) of n device-resident points.
 int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
                std::string *err);
+
+// The engine's per-point f64 -> f32 key conversion over n device values.
+int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStream_t stream, std::string *err);
 
 // Per-mode entry points, instantiated in separate translation units.
 int run_rcb_ref32(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);

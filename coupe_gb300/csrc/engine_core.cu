@@ -126,6 +126,21 @@ int ensure_workspace(DevCtx &C, size_t bytes, std::string *err) {
     return COUPE_ERR_OK;
 }
 
+static __global__ void k_f64_to_f32(const double *__restrict__ in, float *__restrict__ out, uint64_t n) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = KeyF32::from_f64_bits(f64_bits(in[i]));
+}
+
+int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStream_t stream, std::string *err) {
+    cudaStream_t s = stream ? stream : C.stream;
+    if (n == 0) return COUPE_ERR_OK;
+    const unsigned grid = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)C.sms * 8);
+    k_f64_to_f32<<<grid, 256, 0, s>>>(d_in, d_out, n);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return e == cudaSuccess ? COUPE_ERR_OK : cuda_fail(e, "k_f64_to_f32", err);
+}
+
 int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
     st->mode = a.mode;
     switch (a.mode) {

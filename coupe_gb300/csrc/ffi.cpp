@@ -347,6 +347,20 @@ enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double
     return (coupe_err)rc;
 }
 
+enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n, void *stream) {
+    t_err.clear();
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    int rc = cg::f64_to_f32(*C, d_in, d_out, n, (cudaStream_t)stream, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
 void coupe_gpu_last_stats(struct coupe_gpu_stats *out) {
     if (out) *out = t_stats;
 }
@@ -389,6 +403,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
     if (!std::strcmp(name, "fuse_hist")) return &t.fuse_hist;
     if (!std::strcmp(name, "fuse_min_points")) return &t.fuse_min_points;
+    if (!std::strcmp(name, "fuse_max_nbk")) return &t.fuse_max_nbk;
     return nullptr;
 }
 

@@ -158,23 +158,25 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         mx[d] = ord_f64(-1.7976931348623157e308);
     }
     K *outs[3] = {k0, k1, k2};
-    auto point = [&](const double *p, double *q) {
+    // q receives the raw bits of the (mapped) coordinates; without a basis
+    // change nothing here executes an f64 instruction
+    auto point = [&](const double *p, uint64_t *q) {
         if (M.on) {
 #pragma unroll
             for (int r = 0; r < D; ++r) {
                 double acc = __dmul_rn(M.m[r * D + 0], p[0]);
 #pragma unroll
                 for (int c = 1; c < D; ++c) acc = __dadd_rn(acc, __dmul_rn(M.m[r * D + c], p[c]));
-                q[r] = acc;
+                q[r] = f64_bits(acc);
             }
         } else {
 #pragma unroll
-            for (int d = 0; d < D; ++d) q[d] = p[d];
+            for (int d = 0; d < D; ++d) q[d] = f64_bits(p[d]);
         }
 #pragma unroll
         for (int d = 0; d < D; ++d)
-            if (q[d] == q[d]) {
-                const uint64_t o = ord_f64(q[d]);
+            if ((q[d] & 0x7fffffffffffffffull) <= 0x7ff0000000000000ull) {  // not NaN
+                const uint64_t o = (q[d] & 0x8000000000000000ull) ? ~q[d] : (q[d] | 0x8000000000000000ull);
                 mn[d] = o < mn[d] ? o : mn[d];
                 mx[d] = o > mx[d] ? o : mx[d];
             }
@@ -192,26 +194,29 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             flat[2 * v] = t.x;
             flat[2 * v + 1] = t.y;
         }
-        double q[4][D];
+        uint64_t q[4][D];
 #pragma unroll
         for (int j = 0; j < 4; ++j) point(flat + j * D, q[j]);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
+            K o[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) o[j] = KT::from_f64_bits(q[j][d]);
             if (sizeof(K) == 4) {
-                float4 o = make_float4((float)q[0][d], (float)q[1][d], (float)q[2][d], (float)q[3][d]);
-                *(float4 *)((float *)outs[d] + 4 * g) = o;
+                *(uint4 *)((uint32_t *)outs[d] + 4 * g) =
+                    make_uint4(*(uint32_t *)&o[0], *(uint32_t *)&o[1], *(uint32_t *)&o[2], *(uint32_t *)&o[3]);
             } else {
-                double2 *dst = (double2 *)((double *)outs[d] + 4 * g);
-                dst[0] = make_double2(q[0][d], q[1][d]);
-                dst[1] = make_double2(q[2][d], q[3][d]);
+                ulonglong2 *dst = (ulonglong2 *)((unsigned long long *)outs[d] + 4 * g);
+                dst[0] = make_ulonglong2(*(unsigned long long *)&o[0], *(unsigned long long *)&o[1]);
+                dst[1] = make_ulonglong2(*(unsigned long long *)&o[2], *(unsigned long long *)&o[3]);
             }
         }
     }
     for (uint64_t i = groups * 4 + tid; i < n; i += stride) {
-        double q[D];
+        uint64_t q[D];
         point(pts + i * D, q);
 #pragma unroll
-        for (int d = 0; d < D; ++d) outs[d][i] = KT::from_f64(q[d]);
+        for (int d = 0; d < D; ++d) outs[d][i] = KT::from_f64_bits(q[d]);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -353,7 +358,7 @@ struct BinGuess {
 template <class KT>
 __device__ __forceinline__ BinGuess bin_guess(typename KT::T lo, typename KT::T hi, int nb) {
     BinGuess g;
-    const float l = (float)lo, h = (float)hi;
+    const float l = KT::approx(lo), h = KT::approx(hi);
     const float sc = (float)nb / (h - l);
     g.lo = l;
     g.scale = sc;
@@ -364,17 +369,17 @@ __device__ __forceinline__ BinGuess bin_guess(typename KT::T lo, typename KT::T 
 template <class KT>
 __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT::T *cuts, int nb, const BinGuess &g) {
     if (g.fast) {
-        float f = ((float)key - g.lo) * g.scale;
+        float f = (KT::approx(key) - g.lo) * g.scale;
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
         int b = __float2int_rz(f);
-        while (b > 0 && key < cuts[b - 1]) --b;
-        while (b < nb - 1 && !(key < cuts[b])) ++b;
+        while (b > 0 && KT::lt(key, cuts[b - 1])) --b;
+        while (b < nb - 1 && !KT::lt(key, cuts[b])) ++b;
         return b;
     }
     int l = 0, r = nb - 1;
     while (l < r) {
         const int m = (l + r) >> 1;
-        if (key < cuts[m])
+        if (KT::lt(key, cuts[m]))
             r = m;
         else
             l = m + 1;
@@ -472,10 +477,10 @@ __global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs
 #pragma unroll
             for (int i = 0; i < HIST_ITEMS; ++i) {
                 const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
-                if (e < b && kv[i] == kv[i]) {
+                if (e < b && !KT::isnan(kv[i])) {
                     uint64_t q[L];
                     WT::limbs(wv[i], fs, q);
-                    const bool below = kv[i] < lo, above = !below && !(kv[i] < hi);
+                    const bool below = KT::lt(kv[i], lo), above = !below && !KT::lt(kv[i], hi);
                     if (below || above) {
                         // constant indices only: keeps the sums in registers
                         const O v = (O)~KT::ord(kv[i]);
@@ -653,7 +658,8 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         const O kminO = m < kmin_above ? m : kmin_above;
         const K t = KT::mid(lo, hi);
         const K kmin = KT::unord(kminO);
-        const K dist = kmin - t;
+        // distance of the nearest item on the right (recursive_bisection.rs:487)
+        const typename KT::A dist = KT::val(kmin) - KT::val(t);
         ++steps;
         if (!(dist < KT::inf())) {
             // no item on the right of t (recursive_bisection.rs:522-545)
@@ -673,7 +679,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         const V wl = WT::value(wacc, fs);
         const double ideal = WT::f64(sum) / 2.0;
         const double imb = fabs((WT::f64(wl) - ideal) / ideal);
-        if (count == prev || hi <= t + dist || imb <= tol) {
+        if (count == prev || KT::val(hi) <= KT::val(t) + dist || imb <= tol) {
             state = SEG_DONE;
             pivot = kmin;
             split_pos = t;
@@ -875,9 +881,11 @@ struct ReorderArgs {
     RunScalars *rs;
 };
 
+// Staging of one tile: D key tiles, a weight tile and, on the index path,
+// an index tile.
 template <int D, class KT, class WT>
-__host__ __device__ constexpr size_t reorder_stage_smem() {
-    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + sizeof(uint32_t));
+__host__ __device__ constexpr size_t reorder_stage_smem(bool with_index) {
+    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + (with_index ? sizeof(uint32_t) : 0));
 }
 
 // Shared memory of the fused histogram for 2^nbk bins per side.
@@ -888,7 +896,7 @@ __host__ __device__ constexpr size_t reorder_hist_smem(int nbk) {
 
 template <class KT>
 __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg) {
-    return sg.state == SEG_ALLLEFT || key < sg.pivot;
+    return sg.state == SEG_ALLLEFT || KT::lt(key, sg.pivot);
 }
 
 template <class T>
@@ -905,7 +913,7 @@ __device__ __forceinline__ void stage_out(const T *stage, T *dst, uint32_t tcoun
 }
 
 template <int D, class KT, class WT>
-__global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
+__global__ void __launch_bounds__(BLOCK, 3) k_reorder(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
     typedef typename KT::Ord O;
     typedef typename WT::S WS;
@@ -918,7 +926,7 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
     // fused histogram (after the staging): per side 2^nbk_next bins
     const bool fuse = A.hn.cnt != nullptr;
     const int NBn = 1 << A.nbk_next;
-    uint64_t *hw = (uint64_t *)(dsm + reorder_stage_smem<D, KT, WT>());  // [2][NBn][L]
+    uint64_t *hw = (uint64_t *)(dsm + reorder_stage_smem<D, KT, WT>(A.idst != nullptr));  // [2][NBn][L]
     O *hinv = (O *)(hw + 2 * NBn * L);                                   // [2][NBn]
     uint32_t *hcnt = (uint32_t *)(hinv + 2 * NBn);                       // [2][NBn]
     K *cuts = (K *)(hcnt + 2 * NBn);                                     // [NBn - 1]
@@ -1037,7 +1045,7 @@ __global__ void __launch_bounds__(BLOCK) k_reorder(ReorderArgs<D, KT, WT> A) {
                     for (int i = 0; i < R_ITEMS; ++i) {
                         const uint32_t li = i * BLOCK + threadIdx.x;
                         const K key = nc == 0 ? kv[0][i] : (nc == 1 ? kv[1][i] : kv[D - 1][i]);
-                        if (li < tcount && key == key) {
+                        if (li < tcount && !KT::isnan(key)) {
                             const int side = fl[i] ? 0 : 1;
                             const int bin = side * NBn + bin_sorted<KT>(key, cuts, NBn, g);
                             uint64_t q[L];
@@ -1171,7 +1179,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
             const uint64_t j = lv.off[L] + seg;
             const Trav<KT> t = j < cached ? st[j] : trav[j];
             const K kc = c == 0 ? key[0] : (c == 1 ? key[1] : key[D - 1]);
-            const bool left = (t.flags & TRAV_ALLLEFT) || kc < t.pivot;
+            const bool left = (t.flags & TRAV_ALLLEFT) || KT::lt(kc, t.pivot);
             if (L + 1 < levels)
                 seg = t.next + (left ? 0 : ((t.flags & TRAV_HAS_LEFT) ? 1 : 0));
             else

@@ -121,8 +121,9 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
     const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
     const int nbk_max = std::min(hist_max_nbk<WT>(), std::max(1, tu.max_nbk));
-    constexpr size_t r_stage = reorder_stage_smem<D, KT, WT>();
-    const size_t r_smem_max = r_stage + reorder_hist_smem<KT, WT>(nbk_max);
+    const int nbk_fuse = std::min(nbk_max, std::max(1, tu.fuse_max_nbk));
+    const size_t r_stage = reorder_stage_smem<D, KT, WT>(index_path);
+    const size_t r_smem_max = r_stage + reorder_hist_smem<KT, WT>(nbk_fuse);
     CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)r_smem_max));
     const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem_max);
@@ -259,10 +260,10 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         CG_CK(cudaStreamSynchronize(s));
         if (h_rs->err) break;
         const uint64_t S_next = h_rs->nsegs_next;
-        const int nbk_next = pick_nbk(S_next);
         // fuse the next level's first histogram pass into this reorder unless
         // its segments are so small that per-segment set-up would dominate
         const bool fuse = tu.fuse_hist && n >= S_next * (uint64_t)tu.fuse_min_points;
+        const int nbk_next = fuse ? std::min(pick_nbk(S_next), nbk_fuse) : pick_nbk(S_next);
         if (fuse) {
             const uint64_t NBn = 1ull << nbk_next;
             CG_CK(cudaMemsetAsync(B.hcnt, 0, S_next * NBn * sizeof(uint32_t), s));

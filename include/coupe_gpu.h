@@ -82,6 +82,12 @@ enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t 
 enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double *d_points,
 		double *obb_to_aabb, void *stream);
 
+/* The engine's f64 -> f32 key conversion (coupe's `point[coord] as f32`,
+ * coupe/src/algorithms/recursive_bisection.rs:677) applied to n device
+ * values, so that callers can check it against IEEE round-to-nearest-even.
+ * The engine computes it with integer instructions. */
+enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n, void *stream);
+
 /* Copies the statistics of the calling thread's last run. */
 void coupe_gpu_last_stats(struct coupe_gpu_stats *out);
 
@@ -108,6 +114,7 @@ const char *coupe_gpu_kernel_name(int id);
  *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
  *   "fuse_hist"               1: bin the next level inside each reorder
  *   "fuse_min_points"         ... when its segments average this many points
+ *   "fuse_max_nbk"            bisection steps of such a fused pass (1..10)
  * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
 int coupe_gpu_set_option(const char *name, int64_t value);
 

@@ -292,3 +292,34 @@ def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     finally:
         for k, v in old.items():
             coupe.set_option(k, v)
+
+
+def test_key_conversion_is_ieee_rne(coupe):
+    """The engine's integer f64 -> f32 conversion equals IEEE round-to-nearest-
+    even (numpy's cast) on random bit patterns, the f32 range edges, halfway
+    cases and the special values."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(30)
+    bits = [rng.integers(0, 2**64, size=4_000_000, dtype=np.uint64)]
+    e = rng.integers(896 - 40, 1151 + 40, size=2_000_000, dtype=np.uint64)
+    frac = rng.integers(0, 2**52, size=len(e), dtype=np.uint64)
+    sign = rng.integers(0, 2, size=len(e), dtype=np.uint64) << np.uint64(63)
+    bits.append(sign | (e << np.uint64(52)) | frac)
+    half = (sign | (e << np.uint64(52)) | (frac & ~np.uint64((1 << 29) - 1)) | np.uint64(1 << 28))
+    bits += [half, half - np.uint64(1), half + np.uint64(1)]
+    bits.append(np.array([0, 1 << 63, 0x7FF0 << 48, 0xFFF0 << 48, 0x7FF8 << 48, 1, 0x47EFFFFFE0000000,
+                          0x47EFFFFFEFFFFFFF, 0x47EFFFFFF0000000, 0x36A0000000000000, 0x3690000000000000,
+                          0x3690000000000001, 0x380FFFFFE0000000], dtype=np.uint64))
+    b = np.concatenate(bits)
+    x = b.view(np.float64)
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32)
+    d_in = torch.from_numpy(x.copy()).cuda()
+    d_out = torch.empty(len(x), dtype=torch.float32, device="cuda")
+    L = coupe.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    assert L.coupe_gpu_f64_to_f32(d_in.data_ptr(), d_out.data_ptr(), len(x), stream) == 0
+    got = d_out.cpu().numpy()
+    nan = np.isnan(want)
+    assert (np.isnan(got) == nan).all()
+    assert (got[~nan].view(np.uint32) == want[~nan].view(np.uint32)).all()
