@@ -692,7 +692,7 @@ static void householder(const double *el, int dim, double *h) {
         for (int j = 0; j < dim; ++j) h[i * dim + j] = i == j ? 1.0 : 0.0;
     if (par) return;
     const double sign = el[0] > 0.0 ? -1.0 : 1.0;
-    double w[3];
+    double w[16];  // dim <= 16 (the reference's own test uses 6)
     for (int d = 0; d < dim; ++d) w[d] = el[d] + (d == 0 ? sign * nrm : 0.0);
     double wtw = 0.0;
     for (int d = 0; d < dim; ++d) wtw += w[d] * w[d];
