@@ -380,6 +380,7 @@ enum : uint32_t {
     ERR_SCATTER_BOUNDS = 2u,
     ERR_NONFINITE_WEIGHT = 4u,
     ERR_COUNT_MISMATCH = 8u,
+    ERR_TILE_PERM = 16u,  // a reorder tile's permutation left its range
 };
 
 // Device-side scalars of one run.
@@ -400,6 +401,7 @@ struct RunScalars {
     int32_t fscale;
     uint32_t wide;  // nonzero: some weight is not an integer in [0, 2^20)
     uint32_t pad;
+    uint64_t diag[4];  // details of the first failed device check
 };
 
 }  // namespace cg

@@ -34,9 +34,6 @@ struct Tuning {
     int force_index_path = 0;        // 1: carry input indices through every reorder
     int max_nbk = 10;                // bisection steps per histogram pass (2^max_nbk bins)
     int reorder_chunks_per_cta = 1;  // reorder chunks per resident CTA
-    int fuse_hist = 1;               // 1: next level's first histogram pass inside the reorder
-    int fuse_min_points = 4096;      // ... when its segments average at least this many points
-    int fuse_max_nbk = 9;            // bisection steps of a fused pass (its bins share the reorder's smem)
 };
 Tuning &tuning();
 

@@ -401,9 +401,6 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "force_index_path")) return &t.force_index_path;
     if (!std::strcmp(name, "max_nbk")) return &t.max_nbk;
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
-    if (!std::strcmp(name, "fuse_hist")) return &t.fuse_hist;
-    if (!std::strcmp(name, "fuse_min_points")) return &t.fuse_min_points;
-    if (!std::strcmp(name, "fuse_max_nbk")) return &t.fuse_max_nbk;
     return nullptr;
 }
 

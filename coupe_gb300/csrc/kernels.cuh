@@ -606,6 +606,19 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             Tm = m < Tm ? m : Tm;
         }
     }
+    // Every binned key belongs to this segment.  More counts than items means
+    // corrupt bins: no split is taken from them (the host stops the run before
+    // any later kernel could use sizes derived from them).
+    if (warp_sum_u64(Tc) > sg.n) {
+        if (lane == 0) {
+            flags[k] = 0;
+            if (atomicOr(&rs->err, ERR_COUNT_MISMATCH) == 0) {
+                rs->diag[0] = s;
+                rs->diag[1] = sg.n;
+            }
+        }
+        return;
+    }
     bool fine = false;
     int fine_base = 0;
     uint64_t Fc = 0, Fw[L];
@@ -789,7 +802,11 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
         if (s < S) {
             sg = segs[s];
             nl = sg.nleft;
-            nr = sg.n - sg.nleft;
+            if (nl > sg.n) {  // inconsistent split: report, and keep sizes in range
+                atomicOr(&rs->err, ERR_COUNT_MISMATCH);
+                nl = sg.n;
+            }
+            nr = sg.n - nl;
         }
         uint64_t tc;
         const uint64_t ci = block_exscan_u64((nl > 0) + (nr > 0), sh, tc);
@@ -856,7 +873,11 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
 // k_reorder: stable two-way partition of every segment of the level, out of
 // place, one dynamic chunk of the item range per CTA at a time.  A chunk
 // learns how many left items of its first segment precede it by a decoupled
-// look-back over the chunks before it (bounded wait).
+// look-back over the chunks before it (bounded wait).  The chunk is walked in
+// tiles of R_TILE items staged in shared memory by asynchronous copies (the
+// next tile lands while the current one is partitioned); each tile is
+// permuted in shared memory and leaves as two coalesced runs, its left items
+// and its right items.
 // ---------------------------------------------------------------------------
 template <int D, class KT, class WT>
 struct ReorderArgs {
@@ -873,25 +894,21 @@ struct ReorderArgs {
     const uint32_t *isrc;  // NULL: identity
     uint32_t *idst;
     uint64_t *lb;  // look-back words, one per chunk, zeroed
-    // Fused first histogram pass of the next level: both children of a
-    // segment start their search on the same interval (the segment's box on
-    // the next axis), so each item is binned once into its side's bins.
-    Hist<KT, WT> hn;  // next level's bins (zeroed); hn.cnt == NULL: not fused
-    int nbk_next;
     RunScalars *rs;
 };
 
-// Staging of one tile: D key tiles, a weight tile and, on the index path,
-// an index tile.
+// One tile in shared memory: D key tiles, a weight tile and, on the index
+// path, an index tile.
 template <int D, class KT, class WT>
-__host__ __device__ constexpr size_t reorder_stage_smem(bool with_index) {
+__host__ __device__ constexpr size_t reorder_tile_bytes(bool with_index) {
     return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + (with_index ? sizeof(uint32_t) : 0));
 }
 
-// Shared memory of the fused histogram for 2^nbk bins per side.
-template <class KT, class WT>
-__host__ __device__ constexpr size_t reorder_hist_smem(int nbk) {
-    return (size_t)(1 << nbk) * (sizeof(typename KT::T) + 2 * (8 * WT::LIMBS + 4 + sizeof(typename KT::Ord)));
+// Dynamic shared memory of the reorder: two tiles (asynchronous double
+// buffering) and the tile's inverse permutation.
+template <int D, class KT, class WT>
+__host__ __device__ constexpr size_t reorder_smem(bool with_index) {
+    return 2 * reorder_tile_bytes<D, KT, WT>(with_index) + (size_t)R_TILE * sizeof(uint16_t);
 }
 
 template <class KT>
@@ -899,46 +916,69 @@ __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg)
     return sg.state == SEG_ALLLEFT || KT::lt(key, sg.pivot);
 }
 
-template <class T>
-__device__ __forceinline__ void stage_out(const T *stage, T *dst, uint32_t tcount, uint32_t tile_left, uint64_t left_base,
-                                          uint64_t right_base, uint64_t seg_end, uint64_t left_end, RunScalars *rs) {
-    for (uint32_t k = threadIdx.x; k < tcount; k += BLOCK) {
-        uint64_t d = k < tile_left ? left_base + k : right_base + (k - tile_left);
-        bool ok = k < tile_left ? d < left_end : (d >= left_end && d < seg_end);
-        if (ok)
-            dst[d] = stage[k];
-        else
-            atomicOr(&rs->err, ERR_SCATTER_BOUNDS);
-    }
+// Asynchronous global -> shared copies (cp.async); each thread copies its own
+// elements, so a tile arrives while the previous one is processed.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    if (BYTES == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// A tile of a chunk: items [ts, te) of segment kk.
+struct TileRef {
+    uint32_t kk;
+    uint64_t ts, te;
+    bool valid;
+};
+
 template <int D, class KT, class WT>
-__global__ void __launch_bounds__(BLOCK, 3) k_reorder(ReorderArgs<D, KT, WT> A) {
+__global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
-    typedef typename KT::Ord O;
     typedef typename WT::S WS;
-    constexpr int L = WT::LIMBS;
-    // staging: D key tiles, a weight tile and an index tile (dynamic smem)
     extern __shared__ __align__(16) unsigned char dsm[];
-    K *stK = (K *)dsm;
-    WS *stW = (WS *)(dsm + (size_t)D * R_TILE * sizeof(K));
-    uint32_t *stI = (uint32_t *)(dsm + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS));
-    // fused histogram (after the staging): per side 2^nbk_next bins
-    const bool fuse = A.hn.cnt != nullptr;
-    const int NBn = 1 << A.nbk_next;
-    uint64_t *hw = (uint64_t *)(dsm + reorder_stage_smem<D, KT, WT>(A.idst != nullptr));  // [2][NBn][L]
-    O *hinv = (O *)(hw + 2 * NBn * L);                                   // [2][NBn]
-    uint32_t *hcnt = (uint32_t *)(hinv + 2 * NBn);                       // [2][NBn]
-    K *cuts = (K *)(hcnt + 2 * NBn);                                     // [NBn - 1]
-    const bool packed = L == 1 && A.rs->wide == 0;
-    const int fs = L > 1 ? A.rs->fscale : 0;
-    const int nc = A.coord + 1 == D ? 0 : A.coord + 1;
+    const bool with_index = A.idst != nullptr;
+    const size_t tile_bytes = reorder_tile_bytes<D, KT, WT>(with_index);
+    uint16_t *perm = (uint16_t *)(dsm + 2 * tile_bytes);  // tile slot -> item of the tile
     __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
     __shared__ uint64_t sh[33];
     __shared__ uint64_t s_ticket, s_prefix;
     __shared__ uint32_t s_fail;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const K *__restrict__ kc = A.coord == 0 ? A.ksrc[0] : (A.coord == 1 ? A.ksrc[1] : A.ksrc[2]);
+
+    auto tile_keys = [&](int buf, int d) { return (K *)(dsm + buf * tile_bytes) + (size_t)d * R_TILE; };
+    auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K)); };
+    auto tile_i = [&](int buf) {
+        return (uint32_t *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS));
+    };
+    auto prefetch = [&](const TileRef &t, int buf) {
+        const uint32_t cnt = (uint32_t)(t.te - t.ts);
+#pragma unroll
+        for (int i = 0; i < R_ITEMS; ++i) {
+            const uint32_t li = i * BLOCK + threadIdx.x;
+            if (li < cnt) {
+#pragma unroll
+                for (int d = 0; d < D; ++d) cp_async<sizeof(K)>(tile_keys(buf, d) + li, A.ksrc[d] + t.ts + li);
+                cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
+                if (with_index) {
+                    if (A.isrc)
+                        cp_async<4>(tile_i(buf) + li, A.isrc + t.ts + li);
+                    else
+                        tile_i(buf)[li] = (uint32_t)(t.ts + li);
+                }
+            }
+        }
+        cp_async_commit();
+    };
+
     for (;;) {
         if (threadIdx.x == 0) s_ticket = atomicAdd((unsigned long long *)&A.rs->ticket, 1ull);
         __syncthreads();
@@ -947,6 +987,16 @@ __global__ void __launch_bounds__(BLOCK, 3) k_reorder(ReorderArgs<D, KT, WT> A) 
         const uint64_t c0 = t * A.chunk, c1 = min(A.n, c0 + A.chunk);
         const uint32_t kf = seg_index_of<KT>(A.segs, A.S, c0);
         const uint32_t kl = seg_index_of<KT>(A.segs, A.S, c1 - 1);
+        auto piece_end = [&](uint32_t kk) {
+            const Seg<KT> &g = A.segs[kk];
+            return min(c1, g.off + g.n);
+        };
+        TileRef cur;
+        cur.kk = kf;
+        cur.ts = c0;
+        cur.te = min(cur.ts + R_TILE, piece_end(kf));
+        cur.valid = true;
+        prefetch(cur, 0);  // overlaps the count below
         // count the left items of the last piece
         const Seg<KT> sl = A.segs[kl];
         const uint64_t la = max(c0, sl.off);
@@ -990,158 +1040,116 @@ __global__ void __launch_bounds__(BLOCK, 3) k_reorder(ReorderArgs<D, KT, WT> A) 
             s_prefix = prefix;
         }
         __syncthreads();
-        if (s_fail) continue;
+        if (s_fail) {
+            cp_async_wait<0>();  // the prefetched tile must land before the buffer is reused
+            __syncthreads();
+            continue;
+        }
         const uint64_t prefix_first = s_prefix;
-        for (uint32_t kk = kf; kk <= kl; ++kk) {
-            const Seg<KT> sg = A.segs[kk];
-            const uint64_t pa = max(c0, sg.off), pb = min(c1, sg.off + sg.n);
-            uint64_t running = kk == kf ? prefix_first : 0;
-            const uint64_t seg_end = sg.off + sg.n, left_end = sg.off + sg.nleft;
-            BinGuess g;
-            if (fuse) {
-                // the children's interval on the next axis (select, not index:
-                // a runtime index would move the segment record to local memory)
-                const K blo = nc == 0 ? sg.bmin[0] : (nc == 1 ? sg.bmin[1] : sg.bmin[2]);
-                const K bhi = nc == 0 ? sg.bmax[0] : (nc == 1 ? sg.bmax[1] : sg.bmax[2]);
-                __syncthreads();  // the previous piece's flush has read the bins
-                build_sorted_cuts<KT>(blo, bhi, A.nbk_next, cuts);
-                for (int i = threadIdx.x; i < 2 * NBn; i += BLOCK) {
-                    hcnt[i] = 0;
-                    hinv[i] = 0;
-#pragma unroll
-                    for (int l = 0; l < L; ++l) hw[i * L + l] = 0;
-                }
-                g = bin_guess<KT>(blo, bhi, NBn);
-                __syncthreads();
+        Seg<KT> sg;
+        uint64_t running = 0, seg_end = 0, left_end = 0;
+        int tile_no = 0;
+        while (cur.valid) {
+            // the next tile of the chunk (it may start the next segment)
+            TileRef nxt;
+            nxt.valid = false;
+            if (cur.te < piece_end(cur.kk)) {
+                nxt.kk = cur.kk;
+                nxt.ts = cur.te;
+                nxt.valid = true;
+            } else if (cur.kk < kl) {
+                nxt.kk = cur.kk + 1;
+                nxt.ts = A.segs[nxt.kk].off;
+                nxt.valid = true;
             }
-            for (uint64_t ts = pa; ts < pb; ts += R_TILE) {
-                const uint32_t tcount = (uint32_t)min((uint64_t)R_TILE, pb - ts);
-                // all loads of the tile first: one memory round trip per tile
-                K kv[D][R_ITEMS];
-                WS wv[R_ITEMS];
-                uint32_t iv[R_ITEMS];
-#pragma unroll
-                for (int i = 0; i < R_ITEMS; ++i) {
-                    const uint32_t li = i * BLOCK + threadIdx.x;
-                    if (li < tcount) {
-#pragma unroll
-                        for (int d = 0; d < D; ++d) kv[d][i] = A.ksrc[d][ts + li];
-                        wv[i] = A.wsrc[ts + li];
-                        if (A.idst) iv[i] = A.isrc ? A.isrc[ts + li] : (uint32_t)(ts + li);
-                    }
-                }
-                bool fl[R_ITEMS];
-                uint32_t bal[R_ITEMS];
-#pragma unroll
-                for (int i = 0; i < R_ITEMS; ++i) {
-                    const uint32_t li = i * BLOCK + threadIdx.x;
-                    const K key = A.coord == 0 ? kv[0][i] : (A.coord == 1 ? kv[1][i] : kv[D - 1][i]);
-                    fl[i] = li < tcount && goes_left<KT>(key, sg);
-                    bal[i] = __ballot_sync(0xffffffffu, fl[i]);
-                    if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
-                }
-                if (fuse) {
-#pragma unroll
-                    for (int i = 0; i < R_ITEMS; ++i) {
-                        const uint32_t li = i * BLOCK + threadIdx.x;
-                        const K key = nc == 0 ? kv[0][i] : (nc == 1 ? kv[1][i] : kv[D - 1][i]);
-                        if (li < tcount && !KT::isnan(key)) {
-                            const int side = fl[i] ? 0 : 1;
-                            const int bin = side * NBn + bin_sorted<KT>(key, cuts, NBn, g);
-                            uint64_t q[L];
-                            WT::limbs(wv[i], fs, q);
-                            if (packed) {
-                                atomicAdd((unsigned long long *)&hw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
-                            } else {
-                                atomicAdd(&hcnt[bin], 1u);
-#pragma unroll
-                                for (int l = 0; l < L; ++l)
-                                    if (q[l]) atomicAdd((unsigned long long *)&hw[bin * L + l], (unsigned long long)q[l]);
-                            }
-                            const O v = (O)~KT::ord(key);
-                            if (v > hinv[bin]) atomic_max_ord(&hinv[bin], v);
-                        }
-                    }
-                }
-                __syncthreads();
-                if (warp == 0) {
-                    // exclusive scan of R_ITEMS * NWARPS counts in (row, warp) order
-                    constexpr int PER = (R_ITEMS * NWARPS + 31) / 32;
-                    uint32_t v[PER], tot = 0;
-#pragma unroll
-                    for (int j = 0; j < PER; ++j) {
-                        const int idx = lane * PER + j;
-                        v[j] = idx < R_ITEMS * NWARPS ? s_cnt[idx] : 0;
-                        tot += v[j];
-                    }
-                    uint32_t inc = tot;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
-                        if (lane >= o) inc += u;
-                    }
-                    uint32_t run = inc - tot;
-#pragma unroll
-                    for (int j = 0; j < PER; ++j) {
-                        const int idx = lane * PER + j;
-                        if (idx < R_ITEMS * NWARPS) s_cnt[idx] = run;
-                        run += v[j];
-                    }
-                    if (lane == 31) sh[0] = inc;
-                }
-                __syncthreads();
-                const uint32_t tile_left = (uint32_t)sh[0];
-#pragma unroll
-                for (int i = 0; i < R_ITEMS; ++i) {
-                    const uint32_t li = i * BLOCK + threadIdx.x;
-                    if (li < tcount) {
-                        const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & ((1u << lane) - 1));
-                        const uint32_t p = fl[i] ? before : tile_left + (li - before);
-#pragma unroll
-                        for (int d = 0; d < D; ++d) stK[d * R_TILE + p] = kv[d][i];
-                        stW[p] = wv[i];
-                        if (A.idst) stI[p] = iv[i];
-                    }
-                }
-                __syncthreads();
-                const uint64_t left_base = sg.off + running;
-                const uint64_t right_base = sg.off + sg.nleft + (ts - sg.off - running);
-#pragma unroll
-                for (int d = 0; d < D; ++d)
-                    stage_out<K>(stK + d * R_TILE, A.kdst[d], tcount, tile_left, left_base, right_base, seg_end, left_end,
-                                 A.rs);
-                stage_out<WS>(stW, A.wdst, tcount, tile_left, left_base, right_base, seg_end, left_end, A.rs);
-                if (A.idst)
-                    stage_out<uint32_t>(stI, A.idst, tcount, tile_left, left_base, right_base, seg_end, left_end,
-                                        A.rs);
-                __syncthreads();
-                running += tile_left;
+            if (nxt.valid) {
+                nxt.te = min(nxt.ts + R_TILE, piece_end(nxt.kk));
+                prefetch(nxt, (tile_no + 1) & 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
             }
-            if (fuse) {
-                // flush this piece's bins into the two children's bins
-                for (int i = threadIdx.x; i < 2 * NBn; i += BLOCK) {
-                    const int side = i >= NBn;
-                    uint32_t c;
-                    uint64_t wl[L];
-                    if (packed) {
-                        c = (uint32_t)(hw[i] >> PACK_SHIFT);
-                        wl[0] = hw[i] & PACK_WMASK;
-                    } else {
-                        c = hcnt[i];
+            __syncthreads();  // this tile's copies are visible to every thread
+            const int buf = tile_no & 1;
+            if (tile_no == 0 || cur.ts == A.segs[cur.kk].off) {
+                sg = A.segs[cur.kk];
+                running = cur.kk == kf ? prefix_first : 0;
+                seg_end = sg.off + sg.n;
+                left_end = sg.off + sg.nleft;
+            }
+            const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
+            const K *tkc = tile_keys(buf, A.coord);
+            const WS *tw = tile_w(buf);
+            bool fl[R_ITEMS];
+            uint32_t bal[R_ITEMS];
 #pragma unroll
-                        for (int l = 0; l < L; ++l) wl[l] = hw[i * L + l];
-                    }
-                    if (c) {
-                        const uint64_t child = sg.child + (side && sg.nleft > 0 ? 1 : 0);
-                        const size_t gi = (size_t)child * NBn + (i - side * NBn);
-                        atomicAdd(&A.hn.cnt[gi], c);
+            for (int i = 0; i < R_ITEMS; ++i) {
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                fl[i] = li < tcount && goes_left<KT>(tkc[li], sg);
+                bal[i] = __ballot_sync(0xffffffffu, fl[i]);
+                if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                // exclusive scan of R_ITEMS * NWARPS counts in (row, warp) order
+                constexpr int PER = (R_ITEMS * NWARPS + 31) / 32;
+                uint32_t v[PER], tot = 0;
 #pragma unroll
-                        for (int l = 0; l < L; ++l)
-                            if (wl[l]) atomicAdd((unsigned long long *)&A.hn.w[gi * L + l], (unsigned long long)wl[l]);
-                        atomic_max_ord(&A.hn.inv[gi], hinv[i]);
-                    }
+                for (int j = 0; j < PER; ++j) {
+                    const int idx = lane * PER + j;
+                    v[j] = idx < R_ITEMS * NWARPS ? s_cnt[idx] : 0;
+                    tot += v[j];
+                }
+                uint32_t inc = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += u;
+                }
+                uint32_t run = inc - tot;
+#pragma unroll
+                for (int j = 0; j < PER; ++j) {
+                    const int idx = lane * PER + j;
+                    if (idx < R_ITEMS * NWARPS) s_cnt[idx] = run;
+                    run += v[j];
+                }
+                if (lane == 31) sh[0] = inc;
+            }
+            __syncthreads();
+            const uint32_t tile_left = (uint32_t)sh[0];
+#pragma unroll
+            for (int i = 0; i < R_ITEMS; ++i) {
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                if (li < tcount) {
+                    const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & ((1u << lane) - 1));
+                    const uint32_t slot = fl[i] ? before : tile_left + (li - before);
+                    if (slot < tcount)
+                        perm[slot] = (uint16_t)li;
+                    else
+                        atomicOr(&A.rs->err, ERR_TILE_PERM);
                 }
             }
+            __syncthreads();
+            // write the left run and the right run, coalesced
+            const uint64_t left_base = sg.off + running;
+            const uint64_t right_base = sg.off + sg.nleft + (cur.ts - sg.off - running);
+            for (uint32_t k = threadIdx.x; k < tcount; k += BLOCK) {
+                const uint32_t src = perm[k];
+                const uint64_t d = k < tile_left ? left_base + k : right_base + (k - tile_left);
+                const bool ok = k < tile_left ? d < left_end : (d >= left_end && d < seg_end);
+                if (!ok || src >= tcount) {
+                    atomicOr(&A.rs->err, ok ? ERR_TILE_PERM : ERR_SCATTER_BOUNDS);
+                    continue;
+                }
+#pragma unroll
+                for (int dd = 0; dd < D; ++dd) A.kdst[dd][d] = tile_keys(buf, dd)[src];
+                A.wdst[d] = tw[src];
+                if (with_index) A.idst[d] = tile_i(buf)[src];
+            }
+            running += tile_left;
+            __syncthreads();  // the buffer and perm are free again
+            cur = nxt;
+            ++tile_no;
         }
     }
 }

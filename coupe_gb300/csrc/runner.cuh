@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "engine.h"
 #include "kernels.cuh"
@@ -121,15 +122,12 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
     const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
     const int nbk_max = std::min(hist_max_nbk<WT>(), std::max(1, tu.max_nbk));
-    const int nbk_fuse = std::min(nbk_max, std::max(1, tu.fuse_max_nbk));
-    const size_t r_stage = reorder_stage_smem<D, KT, WT>(index_path);
-    const size_t r_smem_max = r_stage + reorder_hist_smem<KT, WT>(nbk_fuse);
+    const size_t r_smem = reorder_smem<D, KT, WT>(index_path);
     CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)r_smem_max));
-    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem_max);
+                               (int)r_smem));
+    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
     uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
-    chunk = std::min<uint64_t>(chunk, PACK_WINDOW);  // a fused piece must fit a packed window
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
     const uint64_t nchunks = (n + chunk - 1) / chunk;
 
@@ -188,7 +186,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         return k;
     };
     int nbk = pick_nbk(1);
-    bool bins_ready = false;  // this level's first pass was fused into the last reorder
+    int err_level = -1;  // level at whose synchronisation a device check was first seen
     Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
     for (uint64_t L = 0; L < iters; ++L) {
         const int coord = (int)(L % D);
@@ -199,17 +197,15 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         Seg<KT> *segs = B.segs[sb];
         int li = 0;  // list / P buffer in use
         uint64_t nlist = S;
-        if (!bins_ready) {
-            CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
-            CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
-            CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
-            CG_LAUNCH(KID_HIST, n * (sk + sw),
-                      k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs));
-            ++st->hist_passes;
-            st->hist_points += n;
-            bytes += n * (sk + sw);
-        }
+        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
+        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
+        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
+        CG_LAUNCH(KID_HIST, n * (sk + sw),
+                  k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
+                                                          n, B.rs));
+        ++st->hist_passes;
+        st->hist_points += n;
+        bytes += n * (sk + sw);
         for (;;) {
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WT::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
@@ -219,7 +215,10 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
                                                          B.P[li ^ 1], B.rs));
             CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
             CG_CK(cudaStreamSynchronize(s));
-            if (h_rs->err) break;
+            if (h_rs->err) {
+                err_level = (int)L;
+                break;
+            }
             if (h_rs->nactive == 0) break;
             li ^= 1;
             nlist = h_rs->nactive;
@@ -258,18 +257,11 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         }
         CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
         CG_CK(cudaStreamSynchronize(s));
-        if (h_rs->err) break;
-        const uint64_t S_next = h_rs->nsegs_next;
-        // fuse the next level's first histogram pass into this reorder unless
-        // its segments are so small that per-segment set-up would dominate
-        const bool fuse = tu.fuse_hist && n >= S_next * (uint64_t)tu.fuse_min_points;
-        const int nbk_next = fuse ? std::min(pick_nbk(S_next), nbk_fuse) : pick_nbk(S_next);
-        if (fuse) {
-            const uint64_t NBn = 1ull << nbk_next;
-            CG_CK(cudaMemsetAsync(B.hcnt, 0, S_next * NBn * sizeof(uint32_t), s));
-            CG_CK(cudaMemsetAsync(B.hw, 0, S_next * NBn * WT::LIMBS * sizeof(uint64_t), s));
-            CG_CK(cudaMemsetAsync(B.hinv, 0, S_next * NBn * sizeof(typename KT::Ord), s));
+        if (h_rs->err) {
+            err_level = (int)L;
+            break;
         }
+        const uint64_t S_next = h_rs->nsegs_next;
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
         const int kb_next = kb == 1 ? 2 : 1;
@@ -289,24 +281,16 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         R.isrc = ic;
         R.idst = index_path ? B.idx[snext] : nullptr;
         R.lb = B.lb;
-        R.hn = fuse ? H : Hist<KT, WT>{nullptr, nullptr, nullptr};
-        R.nbk_next = nbk_next;
         R.rs = B.rs;
-        const size_t r_smem = r_stage + (fuse ? reorder_hist_smem<KT, WT>(nbk_next) : 0);
         const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
         CG_LAUNCH(KID_REORDER, rbytes,
                   k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
         bytes += n * sk /* flag pre-count */ + rbytes;
-        if (fuse) {
-            ++st->hist_passes;
-            st->hist_points += n;
-        }
         kb = kb_next;
         sb = snext;
         level0 = false;
         S = S_next;
-        nbk = nbk_next;
-        bins_ready = fuse;
+        nbk = pick_nbk(S_next);
         st->levels = L + 1;
     }
     CG_CK(cudaEventRecord(C.ev1, s));
@@ -331,7 +315,10 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
             *err = "f64 weights must be finite";
             return COUPE_ERR_BAD_TYPE;
         }
-        *err = std::string("device check failed (code ") + std::to_string(e) + ")";
+        *err = std::string("device check failed (code ") + std::to_string(e) + ", seen at level " +
+               std::to_string(err_level) + " of " + std::to_string(iters) + "; " + std::to_string(h_rs->diag[0]) +
+               " " + std::to_string(h_rs->diag[1]) + " " + std::to_string(h_rs->diag[2]) + " " +
+               std::to_string(h_rs->diag[3]) + ")";
         return COUPE_ERR_CRASH;
     }
     return COUPE_ERR_OK;

@@ -112,9 +112,6 @@ const char *coupe_gpu_kernel_name(int id);
  *                             reorder instead of tracing the recorded splits
  *   "max_nbk"                 bisection steps per histogram pass (1..10)
  *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
- *   "fuse_hist"               1: bin the next level inside each reorder
- *   "fuse_min_points"         ... when its segments average this many points
- *   "fuse_max_nbk"            bisection steps of such a fused pass (1..10)
  * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
 int coupe_gpu_set_option(const char *name, int64_t value);
 

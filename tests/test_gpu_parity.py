@@ -270,7 +270,8 @@ def test_rib_end_to_end(coupe, oracle_mod):
 
 @pytest.mark.parametrize("knobs", [{"force_index_path": 1}, {"max_nbk": 3}, {"max_nbk": 1}, {"max_nbk": 8},
                                    {"reorder_chunks_per_cta": 4}, {"reorder_chunks_per_cta": 64},
-                                   {"fuse_hist": 0}, {"fuse_min_points": 1}, {"fuse_min_points": 1, "max_nbk": 5}])
+                                   {"max_nbk": 5, "reorder_chunks_per_cta": 3},
+                                   {"force_index_path": 1, "reorder_chunks_per_cta": 7}])
 def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     """Part ids through the index path, fewer bisection steps per pass and
     other chunkings equal the oracle's."""
@@ -292,6 +293,28 @@ def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     finally:
         for k, v in old.items():
             coupe.set_option(k, v)
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f64"])
+def test_full_size_repeatable(coupe, oracle_mod, mode):
+    """16.8 M points, 1024 parts (the benchmark workload): equal to the
+    oracle once, then 40 device-resident runs in a row give the same ids and
+    raise no device check (look-back, scatter bounds, tile permutation)."""
+    torch = pytest.importorskip("torch")
+    import os
+    from coupe_gb300 import workloads
+    pts, w, cfg = workloads.gaussian_mixture3d(n=16_777_216, seed=0)
+    want, _ = oracle_mod.rcb(pts, w, 10, 0.01, mode=_oracle_mode(mode), threads=os.cpu_count() or 1)
+    dp = torch.from_numpy(pts).cuda()
+    dw = torch.from_numpy(w).cuda()
+    part = torch.empty(len(pts), dtype=torch.int64, device="cuda")
+    coupe.rcb_device(part, dp, dw, 10, 0.01, mode=mode)
+    first = part.clone()
+    assert (part.cpu().numpy().astype(np.uint64) == want).all()
+    for _ in range(40):
+        part.fill_(-1)
+        coupe.rcb_device(part, dp, dw, 10, 0.01, mode=mode)
+        assert torch.equal(part, first)
 
 
 def test_key_conversion_is_ieee_rne(coupe):
