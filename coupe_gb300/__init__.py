@@ -39,6 +39,7 @@ EXPORTED = [
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
+    "coupe_gpu_split_noalloc",
 ]
 
 

@@ -17,6 +17,7 @@
 #include "../../include/coupe.h"
 #include "../../include/coupe_gpu.h"
 #include "engine.h"
+#include "split_noalloc.h"
 
 struct coupe_data {
     int kind;  // 0 array, 1 constant, 2 callback
@@ -363,6 +364,17 @@ enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n
 
 void coupe_gpu_last_stats(struct coupe_gpu_stats *out) {
     if (out) *out = t_stats;
+}
+
+enum coupe_err coupe_gpu_split_noalloc(uint64_t n, uint64_t dimension, const double *d_points,
+                                       enum coupe_type weight_type, const void *d_weights, uint64_t coord, double cut,
+                                       double *d_out_points, void *d_out_weights, uint64_t *n_left, void *stream) {
+    t_err.clear();
+    const char *msg = "";
+    const int rc = cg::split_noalloc(n, dimension, d_points, weight_type, d_weights, coord, cut, d_out_points,
+                                     d_out_weights, n_left, stream, &msg);
+    if (rc != COUPE_ERR_OK) t_err = msg;  // host memory, error path only
+    return (coupe_err)rc;
 }
 
 const char *coupe_gpu_last_error(void) { return t_err.c_str(); }

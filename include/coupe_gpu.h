@@ -88,6 +88,48 @@ enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double
  * The engine computes it with integer instructions. */
 enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n, void *stream);
 
+/* Stable split of one part of device-resident points by a cut, allocating
+ * nothing.  No counterpart in the reference: coupe moves the points of a part
+ * with an in-place, unstable partition inside Rcb
+ * (coupe/src/algorithms/recursive_bisection.rs:122-181) and has no
+ * allocation-free call.
+ *
+ * Meant for callers that must not allocate device memory once they are
+ * running.  Examples: a mesh or particle code that works within a fixed
+ * device-memory budget, or one that keeps its own kernels running on other
+ * streams while it partitions.  cudaMalloc and cudaFree can synchronise the
+ * whole device, and an allocation can fail once the budget is taken.  This
+ * call uses no cudaMalloc/cudaFree, no pinned host memory and no library
+ * allocator, and creates no stream or event.  Its only scratch is an
+ * 8256-byte static device array inside the library.
+ *
+ * Moves the n points of `d_points` (AoS, `dimension` = 2 or 3 doubles each,
+ * 8-byte aligned) and their n weights (`weight_type`) to `d_out_points` and
+ * `d_out_weights`.  First come, in input order, the points with
+ * point[coord] < cut (an IEEE comparison: a NaN coordinate or a NaN cut goes
+ * right, -0 equals +0); then, in input order, all others.  *n_left (host
+ * memory) receives the number of the former.  The outputs must not overlap
+ * the inputs.  `stream` is a cudaStream_t (NULL: the default stream); the
+ * call returns after its work on it completed.
+ *
+ * Limits: n <= 2^32 - 1; a larger n returns COUPE_ERR_ALLOC before touching
+ * any memory.  The scratch holds 1024 per-chunk counts; chunks grow with n, so
+ * no call needs more.  Each call clears the scratch words that must start at
+ * zero before its kernels run.
+ *
+ * All calls on one device share the scratch.  Calls that overlap in time on
+ * one device (from several threads, or on several streams) race and give
+ * wrong results; serialise them.
+ *
+ * The first call on each device (with that device current) does a one-time
+ * set-up: it looks up the scratch's device address with
+ * cudaGetSymbolAddress and sets the kernels' shared-memory limit.  Make that
+ * first call before any stream capture. */
+enum coupe_err coupe_gpu_split_noalloc(uint64_t n, uint64_t dimension,
+		const double *d_points, enum coupe_type weight_type, const void *d_weights,
+		uint64_t coord, double cut, double *d_out_points, void *d_out_weights,
+		uint64_t *n_left, void *stream);
+
 /* Copies the statistics of the calling thread's last run. */
 void coupe_gpu_last_stats(struct coupe_gpu_stats *out);
 
