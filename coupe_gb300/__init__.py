@@ -175,10 +175,12 @@ def _as_weights(weights, n):
     if np.isscalar(weights):
         weights = np.full(n, weights)
     w = np.asarray(weights)
-    if w.dtype.kind in "iu" and w.dtype not in (np.int32,):
-        w = w.astype(np.int64)
+    # no copy when the caller's array already has a supported type (a copy
+    # would also leave pinned memory for pageable memory)
+    if w.dtype.kind in "iu" and w.dtype != np.int32:
+        w = w.astype(np.int64, copy=False)
     elif w.dtype.kind == "f":
-        w = w.astype(np.float64)
+        w = w.astype(np.float64, copy=False)
     return np.ascontiguousarray(w)
 
 

@@ -64,6 +64,14 @@ CG_HD double unord_f64(uint64_t u) {
 // ---------------------------------------------------------------------------
 CG_HD uint32_t f64bits_to_f32bits(uint64_t b) {
     const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+    const uint64_t x = b & 0x7fffffffffffffffull;
+    if (x - (897ull << 52) < (254ull << 52)) {
+        // f32 exponent 1..254 before rounding: rebias the exponent field and
+        // round the 52-bit fraction to 23 bits, to nearest even; a carry out
+        // of the fraction moves to the next binade (254 -> 255 is +inf)
+        const uint64_t t = x - (896ull << 52);
+        return sign | (uint32_t)((t + 0x0fffffffull + ((t >> 29) & 1)) >> 29);
+    }
     const int e = (int)((b >> 52) & 0x7ff);
     const uint64_t m = b & 0x000fffffffffffffull;
     if (e == 0x7ff) return sign | (m ? 0x7fc00000u : 0x7f800000u);

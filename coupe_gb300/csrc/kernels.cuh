@@ -25,7 +25,8 @@ constexpr int BLOCK = 256;
 constexpr int NWARPS = BLOCK / 32;
 constexpr int MAX_NBK = 10;
 constexpr int MAX_NB = 1 << MAX_NBK;
-constexpr int HIST_ITEMS = 16;               // items per thread per hist iteration
+constexpr int HIST_ITEMS = 8;                // items per thread per hist iteration
+constexpr int CONV_TILE = 2 * BLOCK;          // points per k_convert tile
 constexpr int R_ITEMS = 8;                   // items per thread per reorder tile
 constexpr int R_TILE = BLOCK * R_ITEMS;      // 2048
 constexpr uint64_t LB_AGG = 1ull << 62;      // look-back: aggregate published
@@ -132,6 +133,26 @@ __device__ __forceinline__ void atomic_max_ord(uint64_t *p, uint64_t v) {
     atomicMax((unsigned long long *)p, (unsigned long long)v);
 }
 
+// Asynchronous global -> shared copies (cp.async); each thread copies its own
+// elements, so a tile arrives while the previous one is processed.  4- and
+// 8-byte copies also fill L1 (.ca); 16-byte copies go through L2 only (.cg).
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
+    static_assert(BYTES == 4 || BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+    if (BYTES == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+    else if (BYTES == 8)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 struct Mat {
     double m[9];
     int on;
@@ -181,42 +202,52 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                 mx[d] = o > mx[d] ? o : mx[d];
             }
     };
-    const uint64_t tid = (uint64_t)blockIdx.x * BLOCK + threadIdx.x, stride = (uint64_t)gridDim.x * BLOCK;
-    // groups of 4 points: 16-byte loads of the AoS input, 16-byte key stores
-    const bool vec = ((uintptr_t)pts & 15) == 0;
-    const uint64_t groups = vec ? n / 4 : 0;
-    for (uint64_t g = tid; g < groups; g += stride) {
-        double flat[4 * D];
-        const double2 *src = (const double2 *)(pts + g * 4 * D);
-#pragma unroll
-        for (int v = 0; v < 2 * D; ++v) {
-            const double2 t = src[v];
-            flat[2 * v] = t.x;
-            flat[2 * v + 1] = t.y;
+    // Tiles of CONV_TILE points move to shared memory by asynchronous copies
+    // (the next tile lands while this one is converted): consecutive threads
+    // copy consecutive 16-byte pieces of the AoS input, so the loads are
+    // coalesced; each thread then converts whole points from shared memory
+    // and the SoA key stores are coalesced too.
+    __shared__ __align__(16) double tile[2][CONV_TILE * D];
+    const bool al16 = ((uintptr_t)pts & 15) == 0;
+    const uint64_t ntiles = (n + CONV_TILE - 1) / CONV_TILE;
+    auto prefetch = [&](uint64_t t, int buf) {
+        const uint64_t p0 = t * CONV_TILE;
+        const uint32_t nd = (uint32_t)(min((uint64_t)CONV_TILE, n - p0) * D);  // doubles in the tile
+        const double *src = pts + p0 * D;
+        if (al16) {
+            // the tile starts on a 16-byte boundary (CONV_TILE * D * 8 is a multiple of 16)
+            for (uint32_t q = threadIdx.x; q < nd / 2; q += BLOCK) cp_async<16>(&tile[buf][2 * q], src + 2 * q);
+            if ((nd & 1) && threadIdx.x == 0) cp_async<8>(&tile[buf][nd - 1], src + nd - 1);
+        } else {
+            for (uint32_t q = threadIdx.x; q < nd; q += BLOCK) cp_async<8>(&tile[buf][q], src + q);
         }
-        uint64_t q[4][D];
+        cp_async_commit();
+    };
+    int buf = 0;
+    if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x, 0);
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t tn = t + gridDim.x;
+        if (tn < ntiles) {
+            prefetch(tn, buf ^ 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const uint64_t p0 = t * CONV_TILE;
+        const uint32_t np = (uint32_t)min((uint64_t)CONV_TILE, n - p0);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) point(flat + j * D, q[j]);
+        for (int r = 0; r < CONV_TILE / BLOCK; ++r) {
+            const uint32_t j = r * BLOCK + threadIdx.x;
+            if (j < np) {
+                uint64_t q[D];
+                point(&tile[buf][j * D], q);
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            K o[4];
-#pragma unroll
-            for (int j = 0; j < 4; ++j) o[j] = KT::from_f64_bits(q[j][d]);
-            if (sizeof(K) == 4) {
-                *(uint4 *)((uint32_t *)outs[d] + 4 * g) =
-                    make_uint4(*(uint32_t *)&o[0], *(uint32_t *)&o[1], *(uint32_t *)&o[2], *(uint32_t *)&o[3]);
-            } else {
-                ulonglong2 *dst = (ulonglong2 *)((unsigned long long *)outs[d] + 4 * g);
-                dst[0] = make_ulonglong2(*(unsigned long long *)&o[0], *(unsigned long long *)&o[1]);
-                dst[1] = make_ulonglong2(*(unsigned long long *)&o[2], *(unsigned long long *)&o[3]);
+                for (int d = 0; d < D; ++d) outs[d][p0 + j] = KT::from_f64_bits(q[d]);
             }
         }
-    }
-    for (uint64_t i = groups * 4 + tid; i < n; i += stride) {
-        uint64_t q[D];
-        point(pts + i * D, q);
-#pragma unroll
-        for (int d = 0; d < D; ++d) outs[d][i] = KT::from_f64_bits(q[d]);
+        __syncthreads();  // the buffer is free for the tile after next
+        buf ^= 1;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -416,7 +447,7 @@ __host__ __device__ constexpr int hist_max_nbk() {
 // shared-memory histogram flushed to the segment's global bins.
 // ---------------------------------------------------------------------------
 template <class KT, class WT>
-__global__ void __launch_bounds__(BLOCK) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+__global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
@@ -916,22 +947,6 @@ __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg)
     return sg.state == SEG_ALLLEFT || KT::lt(key, sg.pivot);
 }
 
-// Asynchronous global -> shared copies (cp.async); each thread copies its own
-// elements, so a tile arrives while the previous one is processed.
-template <int BYTES>
-__device__ __forceinline__ void cp_async(void *smem, const void *gmem) {
-    const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-    if (BYTES == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
-
 // A tile of a chunk: items [ts, te) of segment kk.
 struct TileRef {
     uint32_t kk;
@@ -1195,6 +1210,92 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
             c = c + 1 == D ? 0 : c + 1;
         }
         part[i] = id;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_traverse_smem: k_traverse for a table that fits in shared memory (the
+// usual case: 1023 splits for 1024 parts).  The table is staged as arrays:
+// pivots, one 32-bit word per split (index of the first child in the next
+// level | all-left flag << 30 | has-left flag << 31) and the heap ids of the
+// last level.  Each thread walks TRAV_ILP items at once so that their
+// dependent shared-memory lookups overlap.
+// ---------------------------------------------------------------------------
+constexpr int TRAV_ILP = 4;
+constexpr size_t TRAV_SMEM_MAX = 96 * 1024;
+constexpr uint32_t TRAV_NX_ALLLEFT = 1u << 30, TRAV_NX_HASLEFT = 1u << 31, TRAV_NX_INDEX = (1u << 30) - 1;
+
+template <class KT>
+__host__ __device__ constexpr size_t trav_smem_bytes(uint64_t total, uint64_t n_last) {
+    return n_last * sizeof(uint64_t) + total * (sizeof(typename KT::T) + sizeof(uint32_t));
+}
+
+template <int D, class KT>
+__global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restrict__ trav, uint32_t total,
+                                                         LevelOffsets lv, int levels,
+                                                         const typename KT::T *__restrict__ k0,
+                                                         const typename KT::T *__restrict__ k1,
+                                                         const typename KT::T *__restrict__ k2, uint64_t n,
+                                                         uint64_t *__restrict__ part, const RunScalars *rs) {
+    typedef typename KT::T K;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ uint32_t s_off[MAX_TRAV_LEVELS];
+    const uint32_t off_last = (uint32_t)lv.off[levels - 1];
+    uint64_t *s_heap = (uint64_t *)dsm;               // [total - off_last]
+    K *s_piv = (K *)(s_heap + (total - off_last));   // [total]
+    uint32_t *s_nx = (uint32_t *)(s_piv + total);     // [total]
+    for (uint32_t j = threadIdx.x; j < total; j += BLOCK) {
+        const Trav<KT> t = trav[j];
+        const uint32_t fl = ((t.flags & TRAV_ALLLEFT) ? TRAV_NX_ALLLEFT : 0u) | ((t.flags & TRAV_HAS_LEFT) ? TRAV_NX_HASLEFT : 0u);
+        s_piv[j] = t.pivot;
+        if (j < off_last) {
+            s_nx[j] = fl | ((uint32_t)t.next & TRAV_NX_INDEX);
+        } else {
+            s_nx[j] = fl;
+            s_heap[j - off_last] = t.next;
+        }
+    }
+    for (int L = threadIdx.x; L < levels; L += BLOCK) s_off[L] = (uint32_t)lv.off[L];
+    __syncthreads();
+    const uint64_t hmin = rs->min_heap;
+    const uint64_t step = (uint64_t)gridDim.x * BLOCK * TRAV_ILP;
+    for (uint64_t base = (uint64_t)blockIdx.x * BLOCK * TRAV_ILP + threadIdx.x; base < n; base += step) {
+        K key[TRAV_ILP][D];
+        uint32_t seg[TRAV_ILP];
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = base + (uint64_t)k * BLOCK;
+            seg[k] = 0;
+            if (i < n) {
+                key[k][0] = k0[i];
+                key[k][1] = k1[i];
+                if (D == 3) key[k][D - 1] = k2[i];
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d) key[k][d] = K();
+            }
+        }
+        int c = 0;
+        for (int L = 0; L + 1 < levels; ++L) {
+            const uint32_t o = s_off[L];
+#pragma unroll
+            for (int k = 0; k < TRAV_ILP; ++k) {
+                const uint32_t e = o + seg[k];
+                const uint32_t x = s_nx[e];
+                const K kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
+                const bool left = (x & TRAV_NX_ALLLEFT) || KT::lt(kc, s_piv[e]);
+                seg[k] = (x & TRAV_NX_INDEX) + ((!left && (x & TRAV_NX_HASLEFT)) ? 1u : 0u);
+            }
+            c = c + 1 == D ? 0 : c + 1;
+        }
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = base + (uint64_t)k * BLOCK;
+            const uint32_t e = off_last + seg[k];
+            const K kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
+            const bool left = (s_nx[e] & TRAV_NX_ALLLEFT) || KT::lt(kc, s_piv[e]);
+            if (i < n) part[i] = 2 * s_heap[seg[k]] + (left ? 1 : 2) - hmin;
+        }
     }
 }
 

@@ -123,6 +123,8 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
     const int nbk_max = std::min(hist_max_nbk<WT>(), std::max(1, tu.max_nbk));
     const size_t r_smem = reorder_smem<D, KT, WT>(index_path);
+    CG_CK(cudaFuncSetAttribute((const void *)k_traverse_smem<D, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TRAV_SMEM_MAX));
     CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)r_smem));
     const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
@@ -247,9 +249,19 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
                           k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs));
                 bytes += n * (sk + (ic ? 4 : 0) + 8);
             } else {
-                CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
-                          k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters, B.keys[0][0],
-                                                                       B.keys[0][1], B.keys[0][2], n, a.d_part, B.rs));
+                const uint64_t n_last = trav_used - lv.off[iters - 1];
+                const size_t tsm = trav_smem_bytes<KT>(trav_used, n_last);
+                if (tsm <= TRAV_SMEM_MAX) {
+                    CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                              k_traverse_smem<D, KT><<<g_stream, BLOCK, tsm, s>>>(
+                                  B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
+                                  B.keys[0][2], n, a.d_part, B.rs));
+                } else {
+                    CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                              k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters,
+                                                                           B.keys[0][0], B.keys[0][1], B.keys[0][2],
+                                                                           n, a.d_part, B.rs));
+                }
                 bytes += n * (D * sk + 8);
             }
             st->levels = L + 1;
