@@ -299,6 +299,23 @@ struct WtI64 {
     CG_HD static uint64_t bits(V v) { return (uint64_t)v; }
     CG_HD static V from_bits(uint64_t b) { return (int64_t)b; }
 };
+// Integer weights that all lie in [0, 2^16), stored in 16 bits for the level
+// loop (less traffic per item); sums and values follow Base (WtI32: wrapped
+// i32 sums, WtI64: i64 sums), so results are those of Base.
+template <class Base>
+struct WtC16 {
+    typedef uint16_t S;
+    typedef typename Base::V V;
+    static constexpr int LIMBS = 1;
+    static constexpr int CODE = Base::CODE;
+    CG_HD static void limbs(S w, int, uint64_t *l) { l[0] = w; }
+    CG_HD static V value(const uint64_t *l, int s) { return Base::value(l, s); }
+    CG_HD static V sub(V a, V b) { return Base::sub(a, b); }
+    CG_HD static bool less(V a, V b) { return Base::less(a, b); }
+    CG_HD static double f64(V v) { return Base::f64(v); }
+    CG_HD static uint64_t bits(V v) { return Base::bits(v); }
+    CG_HD static V from_bits(uint64_t b) { return Base::from_bits(b); }
+};
 struct WtF64 {
     typedef double S;
     typedef double V;
@@ -407,8 +424,8 @@ struct RunScalars {
     uint64_t splits;
     uint32_t err;
     int32_t fscale;
-    uint32_t wide;  // nonzero: some weight is not an integer in [0, 2^20)
-    uint32_t pad;
+    uint32_t wide;      // nonzero: some weight is not an integer in [0, 2^20)
+    uint32_t narrow16;  // nonzero: some integer weight is not in [0, 2^16)
     uint64_t diag[4];  // details of the first failed device check
 };
 

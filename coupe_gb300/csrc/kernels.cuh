@@ -291,20 +291,29 @@ __device__ __forceinline__ int run_fscale(const RunScalars *rs, uint64_t n) {
 
 // Total weight (recursive_bisection.rs:684), order independent.
 template <class WT>
-__global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict__ w, uint64_t n, RunScalars *rs) {
+__global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict__ w, uint64_t n, RunScalars *rs,
+                                                uint16_t *__restrict__ c16) {
     const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
     uint64_t acc[WT::LIMBS];
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) acc[l] = 0;
-    bool wide = WT::LIMBS > 1;
+    bool wide = WT::LIMBS > 1, not16 = false;
     for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
         const typename WT::S wi = w[i];
         uint64_t q[WT::LIMBS];
         WT::limbs(wi, fs, q);
 #pragma unroll
         for (int l = 0; l < WT::LIMBS; ++l) acc[l] += q[l];
-        if (WT::LIMBS == 1) wide |= !(wi >= 0 && wi < (1 << PACK_WBITS_IN));
+        if constexpr (WT::LIMBS == 1) {
+            wide |= !(wi >= 0 && wi < (1 << PACK_WBITS_IN));
+            if (c16) {
+                // the 16-bit copy of the level loop, used when no weight fails
+                c16[i] = (uint16_t)wi;
+                not16 |= !(wi >= 0 && wi < 65536);
+            }
+        }
     }
+    if (__any_sync(0xffffffffu, not16) && (threadIdx.x & 31) == 0) atomicOr(&rs->narrow16, 1u);
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) {
         uint64_t v = warp_sum_u64(acc[l]);
@@ -928,11 +937,13 @@ struct ReorderArgs {
     RunScalars *rs;
 };
 
-// One tile in shared memory: D key tiles, a weight tile and, on the index
-// path, an index tile.
+// One tile in shared memory: D key tiles, a weight tile (16 bytes of slack:
+// 16-bit weights arrive as the 4-byte words covering the tile) and, on the
+// index path, an index tile.
 template <int D, class KT, class WT>
 __host__ __device__ constexpr size_t reorder_tile_bytes(bool with_index) {
-    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + (with_index ? sizeof(uint32_t) : 0));
+    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + (with_index ? sizeof(uint32_t) : 0)) +
+           16;
 }
 
 // Dynamic shared memory of the reorder: two tiles (asynchronous double
@@ -972,17 +983,30 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
     auto tile_keys = [&](int buf, int d) { return (K *)(dsm + buf * tile_bytes) + (size_t)d * R_TILE; };
     auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K)); };
     auto tile_i = [&](int buf) {
-        return (uint32_t *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS));
+        return (uint32_t *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS) + 16);
     };
+    // weight of item li of a tile starting at ts (16-bit weights start at the
+    // even element at or before ts)
+    auto tile_wt = [&](int buf, uint64_t ts) { return tile_w(buf) + (sizeof(WS) == 2 ? (uint32_t)(ts & 1) : 0u); };
     auto prefetch = [&](const TileRef &t, int buf) {
         const uint32_t cnt = (uint32_t)(t.te - t.ts);
+        if constexpr (sizeof(WS) == 2) {
+            // the 4-byte words covering [ts, te); the last may reach element
+            // te, one past the range: 16-bit weights only ever live in the
+            // engine's 256-byte aligned workspace buffers, where it is readable
+            const uint64_t w0 = t.ts & ~1ull;
+            const uint32_t nw = (uint32_t)((t.te - w0 + 1) >> 1);
+            const uint32_t *src = (const uint32_t *)(A.wsrc + w0);
+            uint32_t *dst = (uint32_t *)tile_w(buf);
+            for (uint32_t q = threadIdx.x; q < nw; q += BLOCK) cp_async<4>(dst + q, src + q);
+        }
 #pragma unroll
         for (int i = 0; i < R_ITEMS; ++i) {
             const uint32_t li = i * BLOCK + threadIdx.x;
             if (li < cnt) {
 #pragma unroll
                 for (int d = 0; d < D; ++d) cp_async<sizeof(K)>(tile_keys(buf, d) + li, A.ksrc[d] + t.ts + li);
-                cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
+                if constexpr (sizeof(WS) != 2) cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
                 if (with_index) {
                     if (A.isrc)
                         cp_async<4>(tile_i(buf) + li, A.isrc + t.ts + li);
@@ -1094,7 +1118,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
             }
             const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
             const K *tkc = tile_keys(buf, A.coord);
-            const WS *tw = tile_w(buf);
+            const WS *tw = tile_wt(buf, cur.ts);
             bool fl[R_ITEMS];
             uint32_t bal[R_ITEMS];
 #pragma unroll

@@ -91,89 +91,47 @@ static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem
     return per * sms;
 }
 
-template <int D, class KT, class WT>
-int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
+// What the set-up of a run hands to its level loop.
+struct RunSetup {
+    uint64_t n = 0, iters = 0, lbcap = 0, bytes = 0;
+    bool index_path = false;
+    cudaStream_t s = nullptr;
+    RunScalars *h_rs = nullptr;
+    int g_stream = 0;
+};
+
+// The level loop of one run; WT is the caller's weight type (it sizes the
+// buffers), WL the type the loop reads (WT, or its 16-bit copy WtC16<WT>).
+template <int D, class KT, class WT, class WL>
+int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err, Buffers<D, KT, WT> &B,
+               const RunSetup &R0, const typename WL::S *w_in) {
     typedef typename KT::T K;
+    typedef typename WL::S WS;
     const Tuning &tu = tuning();
-    const uint64_t n = a.n;
-    cudaStream_t s = a.stream ? a.stream : C.stream;
-    st->points = n;
-    if (n == 0) return COUPE_ERR_OK;
-    if (n > 0xffffffffull) {
-        *err = "more than 2^32 - 1 points";
-        return COUPE_ERR_ALLOC;
-    }
-    if (a.iter_count == 0) {
-        // rcb_recurse with iter_count == 0 stores id 0 everywhere (:589-602)
-        CG_LAUNCH(KID_FILL, n * 8,
-                  k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part,
-                                                                                                            n, 0));
-        CG_CK(cudaStreamSynchronize(s));
-        return COUPE_ERR_OK;
-    }
-    const uint64_t iters = a.iter_count;
-    // segment capacity: a level holds at most min(2^level, n) segments
-    uint64_t scap = iters >= 40 ? n : std::min<uint64_t>(n, 1ull << iters);
-    scap = std::max<uint64_t>(scap, 1);
-    const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
-    // Part ids come from a traversal of the recorded splits unless the tree is
-    // too large to record; then every reorder carries the input indices.
-    uint64_t tcap = 0;
-    for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
-    const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
-    const int nbk_max = std::min(hist_max_nbk<WT>(), std::max(1, tu.max_nbk));
-    const size_t r_smem = reorder_smem<D, KT, WT>(index_path);
+    const uint64_t n = R0.n, iters = R0.iters;
+    const bool index_path = R0.index_path;
+    cudaStream_t s = R0.s;
+    RunScalars *h_rs = R0.h_rs;
+    const int g_stream = R0.g_stream;
+    uint64_t bytes = R0.bytes;
+    const int nbk_max = std::min(hist_max_nbk<WL>(), std::max(1, tu.max_nbk));
+    const size_t r_smem = reorder_smem<D, KT, WL>(index_path);
     CG_CK(cudaFuncSetAttribute((const void *)k_traverse_smem<D, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)TRAV_SMEM_MAX));
-    CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)r_smem));
-    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WT>, C.sms, BLOCK, r_smem);
+    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WL>, C.sms, BLOCK, r_smem);
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
     uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
     const uint64_t nchunks = (n + chunk - 1) / chunk;
-
-    Buffers<D, KT, WT> B;
-    Bump dry{nullptr, 0};
-    const size_t need = B.carve(dry, n, scap, hb, nchunks, index_path, tcap);
-    int rc = ensure_workspace(C, need, err);
-    if (rc != COUPE_ERR_OK) return rc;
-    Bump real{(char *)C.ws, 0};
-    B.carve(real, n, scap, hb, nchunks, index_path, tcap);
-    RunScalars *h_rs = (RunScalars *)C.h_pinned;
-
-    const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
-    const int g_hist = occupancy_grid((const void *)k_hist<KT, WT>, C.sms, BLOCK, 0);
-
-    CG_CK(cudaEventRecord(C.ev0, s));
-    RunScalars init;
-    std::memset(&init, 0, sizeof(init));
-    for (int d = 0; d < 3; ++d) {
-        init.bbox_min_ord[d] = ord_f64(1.7976931348623157e308);
-        init.bbox_max_ord[d] = ord_f64(-1.7976931348623157e308);
+    if (nchunks > R0.lbcap) {
+        *err = "internal: more reorder chunks than look-back words";
+        return COUPE_ERR_CRASH;
     }
-    init.min_heap = ~0ull;
-    *h_rs = init;
-    CG_CK(cudaMemcpyAsync(B.rs, h_rs, sizeof(RunScalars), cudaMemcpyHostToDevice, s));
-
-    Mat M;
-    std::memset(&M, 0, sizeof(M));
-    M.on = a.has_matrix ? 1 : 0;
-    for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
-    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S), si = index_path ? 4 : 0;
-    CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
-              k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
-                                                          B.rs));
-    const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
-    if (WT::LIMBS > 1) {
-        CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs));
-    }
-    CG_LAUNCH(KID_WSUM, n * sw, k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs));
-    CG_LAUNCH(KID_ROOT, 0, k_root<KT, WT><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
-
-    // algorithmic bytes: the input read and the SoA keys written
-    uint64_t bytes = n * (D * 8 + sw) + n * D * sk + n * sw;  // convert + weight sum
-    if (WT::LIMBS > 1) bytes += n * sw;
+    const int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
+    CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
+    const uint64_t sk = sizeof(K), sw = sizeof(WS), si = index_path ? 4 : 0;
 
     int kb = 0;          // key buffer of the current level
     int sb = 0;          // segment table / weight buffer of the current level
@@ -189,28 +147,28 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     };
     int nbk = pick_nbk(1);
     int err_level = -1;  // level at whose synchronisation a device check was first seen
-    Hist<KT, WT> H{B.hcnt, B.hw, B.hinv};
+    Hist<KT, WL> H{B.hcnt, B.hw, B.hinv};
     for (uint64_t L = 0; L < iters; ++L) {
         const int coord = (int)(L % D);
         const uint64_t NB = 1ull << nbk;
         const K *kc = B.keys[kb][coord];
-        const typename WT::S *wc = level0 ? w_in : B.w[sb];
+        const WS *wc = level0 ? w_in : (const WS *)B.w[sb];
         const uint32_t *ic = level0 ? nullptr : B.idx[sb];
         Seg<KT> *segs = B.segs[sb];
         int li = 0;  // list / P buffer in use
         uint64_t nlist = S;
         CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
-        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WT::LIMBS * sizeof(uint64_t), s));
+        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WL::LIMBS * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
         CG_LAUNCH(KID_HIST, n * (sk + sw),
-                  k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
+                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
                                                           n, B.rs));
         ++st->hist_passes;
         st->hist_points += n;
         bytes += n * (sk + sw);
         for (;;) {
-            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WT::LIMBS + sizeof(typename KT::Ord)),
-                      k_decide<KT, WT><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
+            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
+                      k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
                           segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs));
             CG_LAUNCH(KID_SCAN, 0,
                       k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
@@ -225,7 +183,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
             li ^= 1;
             nlist = h_rs->nactive;
             CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
-                      k_hist<KT, WT><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
+                      k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
                                                               nbk, n, B.rs));
             ++st->hist_passes;
             st->hist_points += h_rs->total_active;
@@ -241,7 +199,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
             trav_used += S;
         }
         CG_LAUNCH(KID_CHILDREN, 0,
-                  k_children<KT, WT><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
+                  k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
                                                         B.list[0], B.P[0], n, trav_l, B.rs));
         if (last) {
             if (index_path) {
@@ -277,7 +235,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
         const int kb_next = kb == 1 ? 2 : 1;
-        ReorderArgs<D, KT, WT> R;
+        ReorderArgs<D, KT, WL> R;
         R.segs = segs;
         R.S = (uint32_t)S;
         R.n = n;
@@ -289,14 +247,14 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
             R.kdst[d] = B.keys[kb_next][d];
         }
         R.wsrc = wc;
-        R.wdst = B.w[snext];
+        R.wdst = (WS *)B.w[snext];
         R.isrc = ic;
         R.idst = index_path ? B.idx[snext] : nullptr;
         R.lb = B.lb;
         R.rs = B.rs;
         const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
         CG_LAUNCH(KID_REORDER, rbytes,
-                  k_reorder<D, KT, WT><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
+                  k_reorder<D, KT, WL><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
         bytes += n * sk /* flag pre-count */ + rbytes;
         kb = kb_next;
         sb = snext;
@@ -318,7 +276,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     st->fixed_scale = h_rs->fscale;
     {
         uint64_t lim[4] = {h_rs->wsum_limbs[0], h_rs->wsum_limbs[1], h_rs->wsum_limbs[2], h_rs->wsum_limbs[3]};
-        st->root_weight_sum = WT::f64(WT::value(lim, h_rs->fscale));
+        st->root_weight_sum = WL::f64(WL::value(lim, h_rs->fscale));
     }
     st->algo_bytes = bytes;
     if (h_rs->err) {
@@ -334,6 +292,99 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         return COUPE_ERR_CRASH;
     }
     return COUPE_ERR_OK;
+}
+
+template <int D, class KT, class WT>
+int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
+    typedef typename KT::T K;
+    const Tuning &tu = tuning();
+    const uint64_t n = a.n;
+    cudaStream_t s = a.stream ? a.stream : C.stream;
+    st->points = n;
+    if (n == 0) return COUPE_ERR_OK;
+    if (n > 0xffffffffull) {
+        *err = "more than 2^32 - 1 points";
+        return COUPE_ERR_ALLOC;
+    }
+    if (a.iter_count == 0) {
+        // rcb_recurse with iter_count == 0 stores id 0 everywhere (:589-602)
+        CG_LAUNCH(KID_FILL, n * 8,
+                  k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part,
+                                                                                                            n, 0));
+        CG_CK(cudaStreamSynchronize(s));
+        return COUPE_ERR_OK;
+    }
+    const uint64_t iters = a.iter_count;
+    // segment capacity: a level holds at most min(2^level, n) segments
+    uint64_t scap = iters >= 40 ? n : std::min<uint64_t>(n, 1ull << iters);
+    scap = std::max<uint64_t>(scap, 1);
+    const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
+    // Part ids come from a traversal of the recorded splits unless the tree is
+    // too large to record; then every reorder carries the input indices.
+    uint64_t tcap = 0;
+    for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
+    const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
+    // look-back words: one per reorder chunk; a reorder grid never exceeds 8
+    // CTAs of BLOCK threads per SM, so this capacity fits every weight type
+    const uint64_t lbcap = (uint64_t)C.sms * 8 * (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
+
+    Buffers<D, KT, WT> B;
+    Bump dry{nullptr, 0};
+    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, tcap);
+    int rc = ensure_workspace(C, need, err);
+    if (rc != COUPE_ERR_OK) return rc;
+    Bump real{(char *)C.ws, 0};
+    B.carve(real, n, scap, hb, lbcap, index_path, tcap);
+    RunScalars *h_rs = (RunScalars *)C.h_pinned;
+
+    const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
+
+    CG_CK(cudaEventRecord(C.ev0, s));
+    RunScalars init;
+    std::memset(&init, 0, sizeof(init));
+    for (int d = 0; d < 3; ++d) {
+        init.bbox_min_ord[d] = ord_f64(1.7976931348623157e308);
+        init.bbox_max_ord[d] = ord_f64(-1.7976931348623157e308);
+    }
+    init.min_heap = ~0ull;
+    *h_rs = init;
+    CG_CK(cudaMemcpyAsync(B.rs, h_rs, sizeof(RunScalars), cudaMemcpyHostToDevice, s));
+
+    Mat M;
+    std::memset(&M, 0, sizeof(M));
+    M.on = a.has_matrix ? 1 : 0;
+    for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
+    const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
+    CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
+              k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
+                                                          B.rs));
+    const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
+    if (WT::LIMBS > 1) {
+        CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs));
+    }
+    // integer weights: the weight sum also writes a 16-bit copy into w[0]
+    // (which level 0 does not otherwise use) for the level loop to read when
+    // every weight lies in [0, 2^16)
+    uint16_t *c16 = WT::LIMBS == 1 ? (uint16_t *)B.w[0] : nullptr;
+    CG_LAUNCH(KID_WSUM, n * sw + (c16 ? n * 2 : 0), k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs, c16));
+
+    RunSetup R0;
+    R0.n = n;
+    R0.iters = a.iter_count;
+    R0.index_path = index_path;
+    R0.s = s;
+    R0.h_rs = h_rs;
+    R0.g_stream = g_stream;
+    R0.lbcap = lbcap;
+    // algorithmic bytes: the input read and the SoA keys written
+    R0.bytes = n * (D * 8 + sw) + n * D * sk + n * sw + (c16 ? n * 2 : 0);  // convert + weight sum
+    if (WT::LIMBS > 1) R0.bytes += n * sw;
+    if constexpr (WT::LIMBS == 1) {
+        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+        CG_CK(cudaStreamSynchronize(s));
+        if (h_rs->narrow16 == 0) return run_levels<D, KT, WT, WtC16<WT>>(C, a, st, err, B, R0, c16);
+    }
+    return run_levels<D, KT, WT, WT>(C, a, st, err, B, R0, w_in);
 }
 
 template <class KT>

@@ -210,6 +210,22 @@ def test_int32_wraparound(coupe, oracle_mod):
     _check(coupe, oracle_mod, pts, w, 6, 0.05)
 
 
+@pytest.mark.parametrize("mode", ["ref32", "f64"])
+def test_16bit_weight_copy_boundary(coupe, oracle_mod, mode):
+    """Integer weights in [0, 2^16) run the level loop on a 16-bit copy: the
+    largest such weight, one past it, odd segment offsets, and c_int sums that
+    still wrap at 32 bits."""
+    rng = np.random.default_rng(25)
+    pts = rng.random((100_003, 3))
+    for top in (65535, 65536):
+        w = rng.integers(0, top + 1, size=len(pts), dtype=np.int64)
+        w[::5] = top
+        _check(coupe, oracle_mod, pts, w, 9, 0.01, mode)
+    w32 = np.full(len(pts), 65535, dtype=np.int32)  # total 6.5e9: wraps in i32
+    w32[::3] = 1
+    _check(coupe, oracle_mod, pts, w32, 7, 0.02, mode)
+
+
 def test_f64_weights_wide_range(coupe, oracle_mod):
     rng = np.random.default_rng(24)
     pts = rng.random((50000, 3))
