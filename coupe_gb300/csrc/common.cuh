@@ -426,7 +426,8 @@ struct RunScalars {
     int32_t fscale;
     uint32_t wide;      // nonzero: some weight is not an integer in [0, 2^20)
     uint32_t narrow16;  // nonzero: some integer weight is not in [0, 2^16)
-    uint64_t diag[4];  // details of the first failed device check
+    uint64_t diag[4];      // details of the first failed device check
+    uint64_t pass_points;  // points read by refinement passes (sum over scans)
 };
 
 }  // namespace cg

@@ -460,7 +460,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
-                                                uint64_t n_total, const RunScalars *rs) {
+                                                uint64_t n_total, const RunScalars *rs, int nlist_dev) {
     typedef typename KT::T K;
     typedef typename KT::Ord O;
     constexpr int L = WT::LIMBS;
@@ -472,6 +472,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
     const int NB = 1 << nbk;
     const int fs = L > 1 ? rs->fscale : 0;
     const bool packed = L == 1 && rs->wide == 0;
+    if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass: the list the last scan left
     const uint64_t T = P[nlist];
     const uint64_t c0 = T * blockIdx.x / gridDim.x, c1 = T * (blockIdx.x + 1) / gridDim.x;
     if (c0 >= c1) return;
@@ -606,13 +607,14 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
 template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
-                                                  RunScalars *rs) {
+                                                  RunScalars *rs, int nlist_dev) {
     typedef typename KT::T K;
     typedef typename KT::Ord O;
     typedef typename WT::V V;
     constexpr int L = WT::LIMBS;
     const int lane = threadIdx.x & 31;
     const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
+    if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass (the grid is an upper bound)
     if (k >= nlist) return;
     const uint32_t s = list[k];
     Seg<KT> sg = segs[s];
@@ -796,8 +798,16 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 template <class KT>
 __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
                                                     const uint32_t *__restrict__ flags, uint32_t nlist,
-                                                    uint32_t *list2, uint64_t *P2, RunScalars *rs) {
+                                                    uint32_t *list2, uint64_t *P2, RunScalars *rs, int nlist_dev) {
     __shared__ uint64_t sh[33];
+    __shared__ uint32_t s_nlist;
+    if (nlist_dev) {
+        // a speculative pass: its list is the one the last scan left; read it
+        // before thread 0 overwrites the count below
+        if (threadIdx.x == 0) s_nlist = (uint32_t)rs->nactive;
+        __syncthreads();
+        nlist = s_nlist;
+    }
     uint64_t outc = 0, run = 0;
     for (uint32_t base = 0; base < nlist; base += blockDim.x) {
         const uint32_t k = base + threadIdx.x;
@@ -818,6 +828,7 @@ __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ 
         P2[outc] = run;
         rs->nactive = outc;
         rs->total_active = run;
+        rs->pass_points += run;  // read by the pass that follows
     }
 }
 
@@ -832,6 +843,9 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                                                    uint64_t n_total, Trav<KT> *trav, RunScalars *rs) {
     typedef typename KT::T K;
     __shared__ uint64_t sh[33];
+    // launched right after a speculative pass: nothing to do while a segment
+    // of the level is still searching (the host runs more passes, then this)
+    if (rs->nactive != 0) return;
     uint64_t outc = 0;
     uint64_t hmin = ~0ull;
     const int nc = (coord + 1) % D;

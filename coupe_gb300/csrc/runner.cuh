@@ -155,41 +155,6 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         const WS *wc = level0 ? w_in : (const WS *)B.w[sb];
         const uint32_t *ic = level0 ? nullptr : B.idx[sb];
         Seg<KT> *segs = B.segs[sb];
-        int li = 0;  // list / P buffer in use
-        uint64_t nlist = S;
-        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
-        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WL::LIMBS * sizeof(uint64_t), s));
-        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
-        CG_LAUNCH(KID_HIST, n * (sk + sw),
-                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H, nbk,
-                                                          n, B.rs));
-        ++st->hist_passes;
-        st->hist_points += n;
-        bytes += n * (sk + sw);
-        for (;;) {
-            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
-                      k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
-                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs));
-            CG_LAUNCH(KID_SCAN, 0,
-                      k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
-                                                         B.P[li ^ 1], B.rs));
-            CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
-            CG_CK(cudaStreamSynchronize(s));
-            if (h_rs->err) {
-                err_level = (int)L;
-                break;
-            }
-            if (h_rs->nactive == 0) break;
-            li ^= 1;
-            nlist = h_rs->nactive;
-            CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
-                      k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs));
-            ++st->hist_passes;
-            st->hist_points += h_rs->total_active;
-            bytes += h_rs->total_active * (sk + sw);
-        }
-        if (h_rs->err) break;
         const bool last = L + 1 == iters;
         const int snext = sb ^ 1;
         Trav<KT> *trav_l = nullptr;
@@ -198,9 +163,89 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             trav_l = B.trav + trav_used;
             trav_used += S;
         }
-        CG_LAUNCH(KID_CHILDREN, 0,
-                  k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
-                                                        B.list[0], B.P[0], n, trav_l, B.rs));
+        auto children = [&]() {
+            CG_LAUNCH(KID_CHILDREN, 0,
+                      k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
+                                                            B.list[0], B.P[0], n, trav_l, B.rs));
+            return (int)COUPE_ERR_OK;
+        };
+        const unsigned decide_grid = (unsigned)((S + NWARPS - 1) / NWARPS);
+        const uint64_t decide_bytes = S * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord));
+        // First pass over every point of the level, its decisions, and the
+        // list of segments still searching (list[1]).
+        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
+        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WL::LIMBS * sizeof(uint64_t), s));
+        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
+        CG_LAUNCH(KID_HIST, n * (sk + sw),
+                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], (uint32_t)S, kc, wc, H, nbk, n,
+                                                          B.rs, 0));
+        ++st->hist_passes;
+        st->hist_points += n;
+        bytes += n * (sk + sw);
+        CG_LAUNCH(KID_DECIDE, decide_bytes,
+                  k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
+                                                                 B.flags, B.rs, 0));
+        CG_LAUNCH(KID_SCAN, 0,
+                  k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[0], B.flags, (uint32_t)S, B.list[1], B.P[1], B.rs, 0));
+        // A speculative second pass over list[1] without asking the host how
+        // long it is: its kernels read the count the scan left and return at
+        // once when no segment is searching.  The next scan leaves list[0].
+        CG_LAUNCH(KID_HIST, 0,
+                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1));
+        ++st->hist_passes;
+        CG_LAUNCH(KID_DECIDE, decide_bytes,
+                  k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
+                                                                 B.rs, 1));
+        CG_LAUNCH(KID_SCAN, 0,
+                  k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[1], B.flags, 0, B.list[0], B.P[0], B.rs, 1));
+        // k_children returns at once if a segment is still searching
+        if (!last) {
+            const int rc_ = children();
+            if (rc_ != COUPE_ERR_OK) return rc_;
+        }
+        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+        CG_CK(cudaStreamSynchronize(s));
+        if (h_rs->err) {
+            err_level = (int)L;
+            break;
+        }
+        // rare: splits that need more steps than two passes replay
+        int li = 0;
+        bool more = false;
+        while (h_rs->nactive > 0) {
+            more = true;
+            const uint64_t nlist = h_rs->nactive;
+            CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
+                      k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
+                                                              nbk, n, B.rs, 0));
+            ++st->hist_passes;
+            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
+                      k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
+                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0));
+            CG_LAUNCH(KID_SCAN, 0,
+                      k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
+                                                         B.P[li ^ 1], B.rs, 0));
+            li ^= 1;
+            CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+            CG_CK(cudaStreamSynchronize(s));
+            if (h_rs->err) break;
+        }
+        if (h_rs->err) {
+            err_level = (int)L;
+            break;
+        }
+        if (last || more) {
+            const int rc_ = children();
+            if (rc_ != COUPE_ERR_OK) return rc_;
+        }
+        if (!last && more) {
+            CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+            CG_CK(cudaStreamSynchronize(s));
+            if (h_rs->err) {
+                err_level = (int)L;
+                break;
+            }
+        }
         if (last) {
             if (index_path) {
                 CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
@@ -223,12 +268,6 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                 bytes += n * (D * sk + 8);
             }
             st->levels = L + 1;
-            break;
-        }
-        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
-        CG_CK(cudaStreamSynchronize(s));
-        if (h_rs->err) {
-            err_level = (int)L;
             break;
         }
         const uint64_t S_next = h_rs->nsegs_next;
@@ -278,6 +317,9 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         uint64_t lim[4] = {h_rs->wsum_limbs[0], h_rs->wsum_limbs[1], h_rs->wsum_limbs[2], h_rs->wsum_limbs[3]};
         st->root_weight_sum = WL::f64(WL::value(lim, h_rs->fscale));
     }
+    // refinement passes: the points each scan left for the pass after it
+    st->hist_points += h_rs->pass_points;
+    bytes += h_rs->pass_points * (sk + sw);
     st->algo_bytes = bytes;
     if (h_rs->err) {
         uint32_t e = h_rs->err;
