@@ -128,8 +128,10 @@ CG_HD float f32_from_bits(uint32_t b) {
 // ---------------------------------------------------------------------------
 struct KeyF32 {
     typedef float T;
+    typedef float C;  // cuts, interval bounds, pivots and boxes
     typedef float A;
     typedef uint32_t Ord;
+    static constexpr bool BAND = false;
     static constexpr Ord ORD_INF = 0xff800000u;  // ord_f32(+inf)
     CG_HD static Ord ord(T k) { return ord_f32(k); }
     CG_HD static T unord(Ord u) { return unord_f32(u); }
@@ -142,11 +144,17 @@ struct KeyF32 {
     CG_HD static float approx(T k) { return k; }
     // recursive_bisection.rs:472 — (min + max) / 2.0 in f32
     CG_HD static T mid(T a, T b) { return (a + b) / 2.0f; }
+    CG_HD static C cut_from_f64(double v) { return (float)v; }
+    CG_HD static float approx_cut(C c) { return c; }
+    CG_HD static C cmid(C a, C b) { return mid(a, b); }
+    CG_HD static A cval(C c) { return c; }
 };
 struct KeyF64 {
     typedef uint64_t T;
+    typedef uint64_t C;
     typedef double A;
     typedef uint64_t Ord;
+    static constexpr bool BAND = false;
     static constexpr Ord ORD_INF = 0xfff0000000000000ull;  // code of +inf
     static constexpr T NAN_CODE = ~0ull;
     CG_HD static T enc_bits(uint64_t b) {
@@ -172,7 +180,82 @@ struct KeyF64 {
         return f32_from_bits(s | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
     }
     CG_HD static T mid(T a, T b) { return from_f64((val(a) + val(b)) / 2.0); }
+    CG_HD static C cut_from_f64(double v) { return from_f64(v); }
+    CG_HD static float approx_cut(C c) { return approx(c); }
+    CG_HD static C cmid(C a, C b) { return mid(a, b); }
+    CG_HD static A cval(C c) { return val(c); }
 };
+
+// Band form (COUPE_GPU_F32KEY_F64BAND): the f32 keys k = RN32(x) of the REF32
+// form are streamed, while cuts, interval bounds, split positions and boxes
+// are KeyF64 codes with KeyF64's f64 arithmetic, so every decision is the
+// F64 form's.  For an f64 cut c, k < RD32(c) implies x < c and k > RU32(c)
+// implies x >= c; only k in [RD32(c), RU32(c)] needs the f64 coordinate,
+// which is then read from the input (the band).  The per-bin minimum is kept
+// on keys; the exact f64 minimum is fetched only when a stop test needs it.
+// Deliberately no lt / mid / val: keys and cuts never meet without the band.
+struct KeyBand {
+    typedef float T;
+    typedef uint64_t C;
+    typedef double A;
+    typedef uint32_t Ord;
+    static constexpr bool BAND = true;
+    static constexpr Ord ORD_INF = 0xff800000u;  // ord_f32(+inf)
+    CG_HD static Ord ord(T k) { return ord_f32(k); }
+    CG_HD static T unord(Ord u) { return unord_f32(u); }
+    CG_HD static T from_f64_bits(uint64_t b) { return KeyF32::from_f64_bits(b); }
+    CG_HD static bool isnan(T k) { return !(k == k); }
+    CG_HD static float approx(T k) { return k; }
+    CG_HD static A inf() { return KeyF64::inf(); }
+    CG_HD static C cut_from_f64(double v) { return KeyF64::from_f64(v); }
+    CG_HD static float approx_cut(C c) { return KeyF64::approx(c); }
+    CG_HD static C cmid(C a, C b) { return KeyF64::mid(a, b); }
+    CG_HD static A cval(C c) { return KeyF64::val(c); }
+    CG_HD static bool clt(C a, C b) { return KeyF64::lt(a, b); }
+};
+
+// f32 bounds of an f64 cut code: RD32(c) and RU32(c) (equal when c is an f32).
+struct CutBounds {
+    float lo, hi;
+};
+CG_HD float f32_step(float f, int dir) {  // the neighbouring float (ordered codes are consecutive)
+    return unord_f32(ord_f32(f) + (uint32_t)dir);
+}
+CG_HD CutBounds band_bounds(uint64_t code) {
+    const double c = KeyF64::val(code);
+    const float r = f32_from_bits(f64bits_to_f32bits(f64_bits(c)));  // RN32(c)
+    const double rd = (double)r;
+    CutBounds b;
+    if (rd == c) {
+        b.lo = b.hi = r;
+    } else if (rd < c) {
+        b.lo = r;
+        b.hi = f32_step(r, 1);
+    } else {
+        b.lo = f32_step(r, -1);
+        b.hi = r;
+    }
+    return b;
+}
+// -1: the key proves x < c; +1: it proves x >= c; 0: the band (NaN keys too)
+CG_HD int band_side(float k, const CutBounds &b) { return k < b.lo ? -1 : (k > b.hi ? 1 : 0); }
+// Closed f64 interval holding every x with RN32(x) == k (k not NaN): the
+// midpoints to the neighbouring floats, or beyond the largest float for +-inf.
+CG_HD void band_interval(float k, double &xl, double &xh) {
+    const uint32_t o = ord_f32(k);
+    const double inf = KeyF64::val(KeyF64::ORD_INF);
+    if (o >= 0xff800000u) {  // +inf
+        xl = (double)unord_f32(o - 1);
+        xh = inf;
+    } else if (o <= 0x007fffffu) {  // -inf
+        xl = -inf;
+        xh = (double)unord_f32(o + 1);
+    } else {
+        const double kd = (double)k;
+        xl = (kd + (double)unord_f32(o - 1)) / 2.0;
+        xh = (kd + (double)unord_f32(o + 1)) / 2.0;
+    }
+}
 
 // ---------------------------------------------------------------------------
 // 128-bit fixed-point sums of f64 weights.  For n weights whose largest
@@ -363,7 +446,7 @@ enum : uint32_t { SEG_ACTIVE = 0, SEG_DONE = 1, SEG_ALLLEFT = 2 };
 
 template <class KT>
 struct Seg {
-    typedef typename KT::T K;
+    typedef typename KT::C K;
     uint64_t off;    // first item
     uint64_t heap;   // heap id: children of h are 2h+1 and 2h+2 (wrapping)
     uint64_t sum;    // weight sum (V bits)
@@ -374,7 +457,11 @@ struct Seg {
     uint32_t state;  // SEG_*
     uint32_t steps;  // bisection steps taken so far
     uint32_t child;  // index of the first non-empty child in the next level
+    uint32_t xstate; // band form: X_PENDING when xmin holds an exact minimum
+    uint32_t xkey;   // band form: the f32 key (ordered) whose exact minimum xmin is
     uint32_t pad;
+    uint64_t xcut;   // band form: ... among the items at or right of this cut
+    uint64_t xmin;   // band form: that minimum (f64 ordered code)
     K lo, hi;        // current search interval on this level's axis
     K pivot;         // result: items with key < pivot go left
     K split_pos;     // result: the cut position
@@ -389,9 +476,10 @@ enum : uint32_t { TRAV_ALLLEFT = 1u, TRAV_HAS_LEFT = 2u };
 
 template <class KT>
 struct Trav {
-    typename KT::T pivot;
+    typename KT::C pivot;
     uint32_t flags;
     uint64_t next;
+    float blo, bhi;  // band form: RD32 / RU32 of the pivot
 };
 
 constexpr int MAX_TRAV_LEVELS = 63;
@@ -428,6 +516,9 @@ struct RunScalars {
     uint32_t narrow16;  // nonzero: some integer weight is not in [0, 2^16)
     uint64_t diag[4];      // details of the first failed device check
     uint64_t pass_points;  // points read by refinement passes (sum over scans)
+    uint32_t nexact;       // band form: decisions that waited for an exact minimum
+    uint32_t pad2;
+    unsigned long long band_points;  // band form: f64 coordinates read
 };
 
 }  // namespace cg

@@ -103,6 +103,7 @@ int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStre
 // Per-mode entry points, instantiated in separate translation units.
 int run_rcb_ref32(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
 int run_rcb_f64(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
+int run_rcb_band(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
 
 // Maps a CUDA error to a coupe_err and records a message.
 int cuda_fail(cudaError_t e, const char *what, std::string *err);

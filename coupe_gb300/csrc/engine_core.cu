@@ -148,6 +148,8 @@ int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) 
         return run_rcb_ref32(C, a, st, err);
     case COUPE_GPU_F64:
         return run_rcb_f64(C, a, st, err);
+    case COUPE_GPU_F32KEY_F64BAND:
+        return run_rcb_band(C, a, st, err);
     default:
         if (err) *err = "precision mode not available in this build";
         return COUPE_ERR_BAD_TYPE;

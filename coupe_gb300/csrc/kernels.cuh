@@ -158,6 +158,48 @@ struct Mat {
     int on;
 };
 
+// Where the band form reads an item's f64 coordinate: the input points (AoS)
+// and the basis change k_convert applied to them (rows padded to 3 columns,
+// so that a row is chosen with constant indices, not a runtime one).
+struct BandSrc {
+    const double *pts;
+    double m[3][3];
+    int on;
+    int D;
+    unsigned long long *count;  // coordinates read (the run's band_points)
+};
+inline BandSrc make_band_src(const double *pts, const Mat &M, int D, unsigned long long *count) {
+    BandSrc b;
+    b.pts = pts;
+    b.count = count;
+    b.on = M.on;
+    b.D = D;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) b.m[r][c] = (r < D && c < D) ? M.m[r * D + c] : 0.0;
+    return b;
+}
+enum : uint32_t { X_NONE = 0u, X_PENDING = 1u };
+
+// Ordered f64 code of coordinate `coord` of input point `orig`, computed as
+// k_convert computes it (the same products and sums, in the same order).
+__device__ __forceinline__ uint64_t band_code(const BandSrc &bs, uint64_t orig, int coord) {
+    const double *p = bs.pts + orig * (uint64_t)bs.D;
+    double x;
+    if (bs.on) {
+        const double m0 = coord == 0 ? bs.m[0][0] : (coord == 1 ? bs.m[1][0] : bs.m[2][0]);
+        const double m1 = coord == 0 ? bs.m[0][1] : (coord == 1 ? bs.m[1][1] : bs.m[2][1]);
+        x = __dadd_rn(__dmul_rn(m0, p[0]), __dmul_rn(m1, p[1]));
+        if (bs.D == 3) {
+            const double m2 = coord == 0 ? bs.m[0][2] : (coord == 1 ? bs.m[1][2] : bs.m[2][2]);
+            x = __dadd_rn(x, __dmul_rn(m2, p[2]));
+        }
+    } else {
+        x = p[coord];
+    }
+    atomicAdd(bs.count, 1ull);
+    return KeyF64::from_f64(x);
+}
+
 // ---------------------------------------------------------------------------
 // k_convert: AoS f64 points -> D SoA key arrays (coupe's `point[coord] as
 // f32`, recursive_bisection.rs:674-679), optionally after the Rib basis change
@@ -340,12 +382,16 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
     s.state = SEG_ACTIVE;
     s.steps = 0;
     s.child = 0;
+    s.xstate = 0;
+    s.xkey = 0;
     s.pad = 0;
+    s.xcut = 0;
+    s.xmin = ~0ull;
     for (int d = 0; d < 3; ++d) {
         double a = d < D ? unord_f64(rs->bbox_min_ord[d]) : 0.0;
         double b = d < D ? unord_f64(rs->bbox_max_ord[d]) : 0.0;
-        s.bmin[d] = KT::from_f64(a);
-        s.bmax[d] = KT::from_f64(b);
+        s.bmin[d] = KT::cut_from_f64(a);
+        s.bmax[d] = KT::cut_from_f64(b);
     }
     s.lo = s.bmin[0];
     s.hi = s.bmax[0];
@@ -367,23 +413,32 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
 // `key < c ? left : right`; bins are in key order.
 // ---------------------------------------------------------------------------
 template <class KT>
-__device__ __forceinline__ void build_sorted_cuts(typename KT::T lo, typename KT::T hi, int nbk,
-                                                  typename KT::T *cuts) {
-    typedef typename KT::T K;
-    const int nodes = (1 << nbk) - 1;
-    for (int i = threadIdx.x; i < nodes; i += blockDim.x) {
-        const uint32_t id1 = (uint32_t)i + 1;  // 1-based heap id
-        const int depth = 31 - __clz(id1);
-        const uint32_t p = id1 - (1u << depth);
-        K a = lo, b = hi;
-        for (int l = depth - 1; l >= 0; --l) {
-            K c = KT::mid(a, b);
-            if ((id1 >> l) & 1)
-                a = c;
-            else
-                b = c;
+__device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT::C hi, int nbk,
+                                                  typename KT::C *cuts, float *cb_lo = nullptr,
+                                                  float *cb_hi = nullptr) {
+    typedef typename KT::C K;
+    // One depth of the tree at a time: node (d, p) at in-order rank
+    // r = (2p + 1) h - 1, h = 2^(nbk-1-d), is the midpoint of the cuts at ranks
+    // r - h and r + h (or lo / hi beyond the ends), which are exactly the
+    // ancestors coupe's loop would have reached it from; one midpoint per cut
+    // (f64 midpoints are costly on GB300).  Contains barriers: every thread of
+    // the block calls it.
+    const int nb = 1 << nbk;
+    for (int d = 0; d < nbk; ++d) {
+        const int h = 1 << (nbk - 1 - d);
+        for (int p = threadIdx.x; p < (1 << d); p += blockDim.x) {
+            const int r = (2 * p + 1) * h - 1;
+            const K a = r - h < 0 ? lo : cuts[r - h];
+            const K b = r + h >= nb - 1 ? hi : cuts[r + h];
+            cuts[r] = KT::cmid(a, b);
+            if constexpr (KT::BAND) {
+                // the band form also needs each cut's f32 bounds
+                const CutBounds cb = band_bounds(cuts[r]);
+                cb_lo[r] = cb.lo;
+                cb_hi[r] = cb.hi;
+            }
         }
-        cuts[((2 * p + 1) << (nbk - 1 - depth)) - 1] = KT::mid(a, b);
+        __syncthreads();
     }
 }
 
@@ -396,9 +451,9 @@ struct BinGuess {
 };
 
 template <class KT>
-__device__ __forceinline__ BinGuess bin_guess(typename KT::T lo, typename KT::T hi, int nb) {
+__device__ __forceinline__ BinGuess bin_guess(typename KT::C lo, typename KT::C hi, int nb) {
     BinGuess g;
-    const float l = KT::approx(lo), h = KT::approx(hi);
+    const float l = KT::approx_cut(lo), h = KT::approx_cut(hi);
     const float sc = (float)nb / (h - l);
     g.lo = l;
     g.scale = sc;
@@ -425,6 +480,39 @@ __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT:
             l = m + 1;
     }
     return l;
+}
+
+// Band form: the bin of a key (the number of cuts c with x >= c).  Cuts whose
+// upper bound lies below the key are certainly passed; if the next cut's
+// lower bound does not exceed the key, the f64 code decides from there.
+template <class KT>
+__device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const float *cb_lo, const float *cb_hi, int nb,
+                                        const BinGuess &g, bool &in_band) {
+    int b;
+    if (g.fast) {
+        float f = (k - g.lo) * g.scale;
+        f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
+        b = __float2int_rz(f);
+        while (b > 0 && !(k > cb_hi[b - 1])) --b;
+        while (b < nb - 1 && k > cb_hi[b]) ++b;
+    } else {
+        int l = 0, r = nb - 1;
+        while (l < r) {
+            const int m = (l + r) >> 1;
+            if (k > cb_hi[m])
+                l = m + 1;
+            else
+                r = m;
+        }
+        b = l;
+    }
+    in_band = b < nb - 1 && !(k < cb_lo[b]);  // cut b's band: finish with bin_band_exact
+    return b;
+}
+// The bin from cut b on, from the f64 code.
+__device__ __forceinline__ int bin_band_exact(int b, uint64_t c, const uint64_t *cuts, int nb) {
+    while (b < nb - 1 && !KeyF64::lt(c, cuts[b])) ++b;
+    return b;
 }
 
 // Global histogram slots: [segment][bin]; inv stores ~ord(key) so that an
@@ -460,12 +548,17 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
-                                                uint64_t n_total, const RunScalars *rs, int nlist_dev) {
+                                                uint64_t n_total, const RunScalars *rs, int nlist_dev,
+                                                const uint32_t *__restrict__ isrc, BandSrc bs, int coord,
+                                                Seg<KT> *segs_w) {
     typedef typename KT::T K;
+    typedef typename KT::C CK;
     typedef typename KT::Ord O;
     constexpr int L = WT::LIMBS;
     constexpr int HNB = 1 << hist_max_nbk<WT>();
-    __shared__ K cuts[HNB];
+    constexpr int BNB = KT::BAND ? HNB : 1;
+    __shared__ CK cuts[HNB];
+    __shared__ float cb_lo[BNB], cb_hi[BNB];  // band form: f32 bounds of the cuts
     __shared__ uint64_t sw[HNB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
     __shared__ uint32_t scnt[HNB];
     __shared__ O sinv[HNB];
@@ -484,9 +577,9 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
         const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
         const Seg<KT> &sg = segs[s];
         const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
-        const K lo = sg.lo, hi = sg.hi;
+        const CK lo = sg.lo, hi = sg.hi;
         __syncthreads();
-        if ((int)s != cur_s) build_sorted_cuts<KT>(lo, hi, nbk, cuts);
+        if ((int)s != cur_s) build_sorted_cuts<KT>(lo, hi, nbk, cuts, cb_lo, cb_hi);
         cur_s = (int)s;
         for (int i = threadIdx.x; i < NB; i += BLOCK) {
             scnt[i] = 0;
@@ -496,6 +589,18 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
         }
         __syncthreads();
         const BinGuess g = bin_guess<KT>(lo, hi, NB);
+        // band form: bounds of the interval's ends (f64 work: once per piece)
+        CutBounds blo = {0.f, 0.f}, bhi = {0.f, 0.f};
+        bool xpend = false;  // band form: a decision waits for an exact minimum
+        uint32_t xkey = 0;
+        uint64_t xcut = 0;
+        if constexpr (KT::BAND) {
+            blo = band_bounds(lo);
+            bhi = band_bounds(hi);
+            xpend = sg.xstate == X_PENDING;
+            xkey = sg.xkey;
+            xcut = sg.xcut;
+        }
         // Keys below lo are all in bin 0 and keys >= hi all in bin NB-1 (every
         // cut lies in [lo, hi]).  Once the interval has narrowed, most keys are
         // there, so they are summed in registers instead of by atomics.
@@ -515,6 +620,98 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
                     wv[i] = wts[e];
                 }
             }
+            if constexpr (KT::BAND) {
+                // f32 keys against f64 cuts: the key decides, except in the
+                // band.  Items in a band (or the key a decision of this segment
+                // waits for) are only marked here, so that this unrolled loop
+                // stays small and keeps the keys in registers; the loop after
+                // it reads their f64 coordinate.
+                uint32_t slow = 0;
+#pragma unroll
+                for (int i = 0; i < HIST_ITEMS; ++i) {
+                    const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                    if (e < b && !KT::isnan(kv[i])) {
+                        if (xpend && KT::ord(kv[i]) == xkey) {
+                            slow |= 1u << i;
+                            continue;
+                        }
+                        const int sl = band_side(kv[i], blo), sh = band_side(kv[i], bhi);
+                        bool in_band = sl == 0 || (sl > 0 && sh == 0);
+                        int bin = 0;
+                        if (sl > 0 && sh < 0) bin = bin_band<KT>(kv[i], cuts, cb_lo, cb_hi, NB, g, in_band);
+                        if (in_band) {
+                            slow |= 1u << i;
+                            continue;
+                        }
+                        uint64_t q[L];
+                        WT::limbs(wv[i], fs, q);
+                        const O v = (O)~KT::ord(kv[i]);
+                        if (sl < 0 || sh > 0) {
+                            // constant indices only: keeps the sums in registers
+                            if (sl < 0) {
+                                out_c[0] += 1;
+#pragma unroll
+                                for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
+                                out_inv[0] = v > out_inv[0] ? v : out_inv[0];
+                            } else {
+                                out_c[1] += 1;
+#pragma unroll
+                                for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
+                                out_inv[1] = v > out_inv[1] ? v : out_inv[1];
+                            }
+                            continue;
+                        }
+                        if (packed) {
+                            atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+                        } else {
+                            atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                            for (int l = 0; l < L; ++l)
+                                if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
+                        }
+                        if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+                    }
+                }
+                while (slow) {
+                    const int i = __ffs(slow) - 1;
+                    slow &= slow - 1;
+                    const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                    const K kk = keys[e];
+                    const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
+                    if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut))
+                        atomicMin((unsigned long long *)&segs_w[s].xmin, (unsigned long long)c);
+                    uint64_t q[L];
+                    WT::limbs(wts[e], fs, q);
+                    const O v = (O)~KT::ord(kk);
+                    const bool below = KeyF64::lt(c, lo), above = !below && !KeyF64::lt(c, hi);
+                    if (below) {
+                        out_c[0] += 1;
+#pragma unroll
+                        for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
+                        out_inv[0] = v > out_inv[0] ? v : out_inv[0];
+                        continue;
+                    }
+                    if (above) {
+                        out_c[1] += 1;
+#pragma unroll
+                        for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
+                        out_inv[1] = v > out_inv[1] ? v : out_inv[1];
+                        continue;
+                    }
+                    bool unused;
+                    const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cb_lo, cb_hi, NB, g, unused), c, cuts, NB);
+                    if (packed) {
+                        atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+                    } else {
+                        atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
+                    }
+                    if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+                }
+                continue;
+            } else {
 #pragma unroll
             for (int i = 0; i < HIST_ITEMS; ++i) {
                 const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
@@ -550,6 +747,7 @@ __global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ s
                     const O v = (O)~KT::ord(kv[i]);
                     if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
                 }
+            }
             }
         }
         // fold the out-of-interval sums into the edge bins (one lane per warp)
@@ -608,10 +806,12 @@ template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
                                                   RunScalars *rs, int nlist_dev) {
-    typedef typename KT::T K;
+    typedef typename KT::C K;  // cuts and interval bounds
     typedef typename KT::Ord O;
     typedef typename WT::V V;
     constexpr int L = WT::LIMBS;
+    // band form: empty bins hold no key at all (not +inf, a possible key)
+    constexpr O NONE = KT::BAND ? (O)~(O)0 : KT::ORD_INF;
     const int lane = threadIdx.x & 31;
     const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
     if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass (the grid is an upper bound)
@@ -631,10 +831,10 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 #pragma unroll
         for (int l = 0; l < L; ++l) w[l] = H.w[g * L + l];
         const O o = (O)~H.inv[g];
-        m = o > KT::ORD_INF ? KT::ORD_INF : o;
+        m = KT::BAND ? o : (o > KT::ORD_INF ? KT::ORD_INF : o);
     };
     uint64_t Tc = 0, Tw[L];
-    O Tm = KT::ORD_INF;
+    O Tm = NONE;
 #pragma unroll
     for (int l = 0; l < L; ++l) Tw[l] = 0;
     if (lane * BS < NB) {
@@ -664,7 +864,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     bool fine = false;
     int fine_base = 0;
     uint64_t Fc = 0, Fw[L];
-    O Fm = KT::ORD_INF;
+    O Fm = NONE;
 #pragma unroll
     for (int l = 0; l < L; ++l) Fw[l] = 0;
 
@@ -676,7 +876,10 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     uint64_t w_below[L];
 #pragma unroll
     for (int l = 0; l < L; ++l) w_below[l] = 0;
-    O kmin_above = KT::ORD_INF;
+    O kmin_above = NONE;
+    bool flag_exact = false;  // band form: a test needs an exact minimum first
+    K xcut = 0;
+    O xkey = 0;
     uint32_t state = SEG_ACTIVE;
     uint32_t steps = 0;
     K pivot = 0, split_pos = 0;
@@ -693,7 +896,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         const int u0 = fine ? fine_base + lane : lane * BS;
         const bool has = fine ? lane < BS : u0 < NB;
         uint64_t c = 0, wp[L];
-        O m = KT::ORD_INF;
+        O m = NONE;
 #pragma unroll
         for (int l = 0; l < L; ++l) wp[l] = 0;
         if (has && u0 >= lo_b && u0 < mid_b) {
@@ -711,12 +914,31 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 #pragma unroll
         for (int l = 0; l < L; ++l) wacc[l] = w_below[l] + wp[l];
         const O kminO = m < kmin_above ? m : kmin_above;
-        const K t = KT::mid(lo, hi);
-        const K kmin = KT::unord(kminO);
-        // distance of the nearest item on the right (recursive_bisection.rs:487)
-        const typename KT::A dist = KT::val(kmin) - KT::val(t);
+        const K t = KT::cmid(lo, hi);
+        const typename KT::A tv = KT::cval(t), hv = KT::cval(hi);
+        // distance of the nearest item on the right (recursive_bisection.rs:487):
+        // exact, or in the band form bounds [dl, dh] of it
+        typename KT::A dl, dh;
+        if constexpr (KT::BAND) {
+            if (kminO == NONE) {
+                dl = dh = KT::inf();
+            } else {
+                double xl, xh;
+                band_interval(KT::unord(kminO), xl, xh);
+                if (xl < tv) xl = tv;  // items right of t are >= t (the bins are exact)
+                if (xh < xl) xh = xl;
+                if (sg.xstate == X_PENDING && sg.xcut == t && sg.xkey == (uint32_t)kminO && sg.xmin != ~0ull)
+                    xl = xh = KeyF64::val(sg.xmin);  // found by the pass that just ran
+                dl = xl - tv;
+                dh = xh - tv;
+            }
+        } else {
+            dl = dh = KT::cval(KT::unord(kminO)) - tv;
+        }
         ++steps;
-        if (!(dist < KT::inf())) {
+        if (KT::BAND && !(dl < KT::inf()) != !(dh < KT::inf())) {
+            flag_exact = true;  // is there an item right of t at all? (a +inf key)
+        } else if (!(dl < KT::inf())) {
             // no item on the right of t (recursive_bisection.rs:522-545)
             if (prev == count) {
                 state = SEG_ALLLEFT;
@@ -731,12 +953,36 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             kmin_above = kminO;
             continue;
         }
+        if (flag_exact) {
+            --steps;  // this step is replayed once the minimum is exact
+            xcut = t;
+            xkey = kminO;
+            if (sg.xstate == X_PENDING && sg.xcut == t && sg.xkey == (uint32_t)kminO && lane == 0)
+                atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // its resolution found no item
+            break;
+        }
         const V wl = WT::value(wacc, fs);
         const double ideal = WT::f64(sum) / 2.0;
         const double imb = fabs((WT::f64(wl) - ideal) / ideal);
-        if (count == prev || KT::val(hi) <= KT::val(t) + dist || imb <= tol) {
+        // recursive_bisection.rs:547-563; `hi <= t + dist` is monotone in dist
+        const bool near_lo = hv <= tv + dl, near_hi = hv <= tv + dh;
+        if (!(count == prev || imb <= tol) && near_lo != near_hi) {
+            flag_exact = true;
+            --steps;
+            xcut = t;
+            xkey = kminO;
+            if (sg.xstate == X_PENDING && sg.xcut == t && sg.xkey == (uint32_t)kminO && lane == 0)
+                atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // its resolution found no item
+            break;
+        }
+        if (count == prev || near_lo || imb <= tol) {
             state = SEG_DONE;
-            pivot = kmin;
+            // items with key < pivot go left; in the band form the cut itself
+            // (no item lies in [t, min right), so x < t is the same set)
+            if constexpr (KT::BAND)
+                pivot = t;
+            else
+                pivot = KT::unord(kminO);
             split_pos = t;
             wl_out = wl;
             nleft = count;
@@ -768,6 +1014,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             o.lo = lo;
             o.hi = hi;
             o.prev = prev;
+            if (KT::BAND) o.xstate = X_NONE;
             flags[k] = 0;
             atomicAdd((unsigned long long *)&rs->steps_total, (unsigned long long)total_steps);
             atomicMax((unsigned long long *)&rs->steps_max, (unsigned long long)total_steps);
@@ -788,6 +1035,15 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             o.hi = hi;
             o.prev = prev;
             o.steps = total_steps;
+            if (KT::BAND && flag_exact) {
+                o.xstate = X_PENDING;
+                o.xcut = xcut;
+                o.xkey = (uint32_t)xkey;
+                o.xmin = ~0ull;
+                atomicAdd(&rs->nexact, 1u);
+            } else if (KT::BAND) {
+                o.xstate = X_NONE;
+            }
             flags[k] = 1;
         }
     }
@@ -873,6 +1129,12 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                 t.pivot = sg.pivot;
                 t.flags = (sg.state == SEG_ALLLEFT ? TRAV_ALLLEFT : 0u) | (nl > 0 ? TRAV_HAS_LEFT : 0u);
                 t.next = write ? outc + ci : sg.heap;
+                t.blo = t.bhi = 0.f;
+                if constexpr (KT::BAND) {
+                    const CutBounds cb = band_bounds(sg.pivot);
+                    t.blo = cb.lo;
+                    t.bhi = cb.hi;
+                }
                 trav[s] = t;
             }
             if (write) segs[s].child = (uint32_t)(outc + ci);
@@ -893,7 +1155,11 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                     ch.state = SEG_ACTIVE;
                     ch.steps = 0;
                     ch.child = 0;
+                    ch.xstate = 0;
+                    ch.xkey = 0;
                     ch.pad = 0;
+                    ch.xcut = 0;
+                    ch.xmin = ~0ull;
                     for (int d = 0; d < 3; ++d) {
                         ch.bmin[d] = sg.bmin[d];
                         ch.bmax[d] = sg.bmax[d];
@@ -949,27 +1215,39 @@ struct ReorderArgs {
     uint32_t *idst;
     uint64_t *lb;  // look-back words, one per chunk, zeroed
     RunScalars *rs;
+    BandSrc bs;    // band form: the f64 coordinates (through isrc)
 };
 
-// One tile in shared memory: D key tiles, a weight tile (16 bytes of slack:
-// 16-bit weights arrive as the 4-byte words covering the tile) and, on the
-// index path, an index tile.
+// One tile in shared memory: D key tiles and a weight tile (16 bytes of
+// slack: 16-bit weights arrive as the 4-byte words covering the tile).
+// Carried input indices are not double buffered: each thread loads its own
+// items' indices into registers when the tile starts (overlapping the
+// partition work) and parks them in one shared array for the output loop.
 template <int D, class KT, class WT>
-__host__ __device__ constexpr size_t reorder_tile_bytes(bool with_index) {
-    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S) + (with_index ? sizeof(uint32_t) : 0)) +
-           16;
+__host__ __device__ constexpr size_t reorder_tile_bytes() {
+    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S)) + 16;
 }
 
 // Dynamic shared memory of the reorder: two tiles (asynchronous double
-// buffering) and the tile's inverse permutation.
+// buffering), the tile's inverse permutation and, when indices are carried,
+// the tile's indices.
 template <int D, class KT, class WT>
 __host__ __device__ constexpr size_t reorder_smem(bool with_index) {
-    return 2 * reorder_tile_bytes<D, KT, WT>(with_index) + (size_t)R_TILE * sizeof(uint16_t);
+    return 2 * reorder_tile_bytes<D, KT, WT>() + (size_t)R_TILE * sizeof(uint16_t) +
+           (with_index ? (size_t)R_TILE * sizeof(uint32_t) : 0);
 }
 
 template <class KT>
 __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg) {
     return sg.state == SEG_ALLLEFT || KT::lt(key, sg.pivot);
+}
+// Band form: x < pivot (the split cut), from the key unless it lies in the
+// cut's band; `code` then supplies the item's f64 code.
+template <class KT, class CodeFn>
+__device__ __forceinline__ bool goes_left_band(float key, const Seg<KT> &sg, const CutBounds &pb, CodeFn code) {
+    if (sg.state == SEG_ALLLEFT) return true;
+    const int sd = band_side(key, pb);
+    return sd < 0 || (sd == 0 && KeyF64::lt(code(), sg.pivot));
 }
 
 // A tile of a chunk: items [ts, te) of segment kk.
@@ -979,14 +1257,19 @@ struct TileRef {
     bool valid;
 };
 
-template <int D, class KT, class WT>
-__global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) {
+// IDX: the reorder also carries input indices (isrc -> idst); a compile-time
+// choice, so that reorders without indices spend no registers on them.  With
+// 4-byte keys three CTAs fit an SM's shared memory; the bound keeps the
+// registers within that too.
+template <int D, class KT, class WT, bool IDX>
+__global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_reorder(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
     typedef typename WT::S WS;
     extern __shared__ __align__(16) unsigned char dsm[];
-    const bool with_index = A.idst != nullptr;
-    const size_t tile_bytes = reorder_tile_bytes<D, KT, WT>(with_index);
+    constexpr bool with_index = IDX;
+    const size_t tile_bytes = reorder_tile_bytes<D, KT, WT>();
     uint16_t *perm = (uint16_t *)(dsm + 2 * tile_bytes);  // tile slot -> item of the tile
+    uint32_t *s_idx = (uint32_t *)(perm + R_TILE);          // carried indices of the tile (item order)
     __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
     __shared__ uint64_t sh[33];
     __shared__ uint64_t s_ticket, s_prefix;
@@ -996,8 +1279,16 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
 
     auto tile_keys = [&](int buf, int d) { return (K *)(dsm + buf * tile_bytes) + (size_t)d * R_TILE; };
     auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K)); };
-    auto tile_i = [&](int buf) {
-        return (uint32_t *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K) + (size_t)R_TILE * sizeof(WS) + 16);
+    // input index of the item at position e of the level (identity on level 0)
+    auto orig = [&](uint64_t e) { return A.isrc ? (uint64_t)A.isrc[e] : e; };
+    // carried indices of this thread's items of a tile (loaded one tile ahead)
+    auto load_ix = [&](const TileRef &t, uint32_t *ix) {
+        const uint32_t cnt = (uint32_t)(t.te - t.ts);
+#pragma unroll
+        for (int i = 0; i < R_ITEMS; ++i) {
+            const uint32_t li = i * BLOCK + threadIdx.x;
+            ix[i] = li < cnt ? (uint32_t)orig(t.ts + li) : 0u;
+        }
     };
     // weight of item li of a tile starting at ts (16-bit weights start at the
     // even element at or before ts)
@@ -1021,12 +1312,6 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
 #pragma unroll
                 for (int d = 0; d < D; ++d) cp_async<sizeof(K)>(tile_keys(buf, d) + li, A.ksrc[d] + t.ts + li);
                 if constexpr (sizeof(WS) != 2) cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
-                if (with_index) {
-                    if (A.isrc)
-                        cp_async<4>(tile_i(buf) + li, A.isrc + t.ts + li);
-                    else
-                        tile_i(buf)[li] = (uint32_t)(t.ts + li);
-                }
             }
         }
         cp_async_commit();
@@ -1050,11 +1335,22 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
         cur.te = min(cur.ts + R_TILE, piece_end(kf));
         cur.valid = true;
         prefetch(cur, 0);  // overlaps the count below
+        uint32_t ixn[R_ITEMS];  // indices of the next tile to process
+        if (with_index) load_ix(cur, ixn);
         // count the left items of the last piece
         const Seg<KT> sl = A.segs[kl];
         const uint64_t la = max(c0, sl.off);
         uint64_t cnt = 0;
-        for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK) cnt += goes_left<KT>(kc[e], sl) ? 1 : 0;
+        if constexpr (KT::BAND) {
+            const CutBounds pb = band_bounds(sl.pivot);
+            for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK)
+                cnt += goes_left_band<KT>(kc[e], sl, pb,
+                                          [&]() { return band_code(A.bs, A.isrc ? A.isrc[e] : e, A.coord); })
+                           ? 1
+                           : 0;
+        } else {
+            for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK) cnt += goes_left<KT>(kc[e], sl) ? 1 : 0;
+        }
         uint64_t agg;
         block_exscan_u64(cnt, sh, agg);
         const Seg<KT> sf = A.segs[kf];
@@ -1100,6 +1396,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
         }
         const uint64_t prefix_first = s_prefix;
         Seg<KT> sg;
+        CutBounds pb = {0.f, 0.f};  // band form: bounds of sg.pivot
         uint64_t running = 0, seg_end = 0, left_end = 0;
         int tile_no = 0;
         while (cur.valid) {
@@ -1126,6 +1423,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
             const int buf = tile_no & 1;
             if (tile_no == 0 || cur.ts == A.segs[cur.kk].off) {
                 sg = A.segs[cur.kk];
+                if constexpr (KT::BAND) pb = band_bounds(sg.pivot);
                 running = cur.kk == kf ? prefix_first : 0;
                 seg_end = sg.off + sg.n;
                 left_end = sg.off + sg.nleft;
@@ -1133,12 +1431,23 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
             const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
             const K *tkc = tile_keys(buf, A.coord);
             const WS *tw = tile_wt(buf, cur.ts);
+            uint32_t ix[R_ITEMS];  // carried indices of this thread's items
+            if (with_index) {
+#pragma unroll
+                for (int i = 0; i < R_ITEMS; ++i) ix[i] = ixn[i];
+                if (nxt.valid) load_ix(nxt, ixn);
+            }
             bool fl[R_ITEMS];
             uint32_t bal[R_ITEMS];
 #pragma unroll
             for (int i = 0; i < R_ITEMS; ++i) {
                 const uint32_t li = i * BLOCK + threadIdx.x;
-                fl[i] = li < tcount && goes_left<KT>(tkc[li], sg);
+                if constexpr (KT::BAND)
+                    fl[i] = li < tcount && goes_left_band<KT>(tkc[li], sg, pb, [&]() {
+                                return band_code(A.bs, ix[i], A.coord);
+                            });
+                else
+                    fl[i] = li < tcount && goes_left<KT>(tkc[li], sg);
                 bal[i] = __ballot_sync(0xffffffffu, fl[i]);
                 if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
             }
@@ -1180,6 +1489,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
                         perm[slot] = (uint16_t)li;
                     else
                         atomicOr(&A.rs->err, ERR_TILE_PERM);
+                    if (with_index) s_idx[li] = ix[i];
                 }
             }
             __syncthreads();
@@ -1197,7 +1507,7 @@ __global__ void __launch_bounds__(BLOCK, 2) k_reorder(ReorderArgs<D, KT, WT> A) 
 #pragma unroll
                 for (int dd = 0; dd < D; ++dd) A.kdst[dd][d] = tile_keys(buf, dd)[src];
                 A.wdst[d] = tw[src];
-                if (with_index) A.idst[d] = tile_i(buf)[src];
+                if (with_index) A.idst[d] = s_idx[src];
             }
             running += tile_left;
             __syncthreads();  // the buffer and perm are free again
@@ -1221,7 +1531,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
                                                     LevelOffsets lv, int levels, const typename KT::T *__restrict__ k0,
                                                     const typename KT::T *__restrict__ k1,
                                                     const typename KT::T *__restrict__ k2, uint64_t n,
-                                                    uint64_t *__restrict__ part, const RunScalars *rs) {
+                                                    uint64_t *__restrict__ part, const RunScalars *rs, BandSrc bs) {
     typedef typename KT::T K;
     constexpr int CAP = TRAV_SMEM_BYTES / sizeof(Trav<KT>);
     __shared__ Trav<KT> st[CAP];
@@ -1240,7 +1550,15 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
             const uint64_t j = lv.off[L] + seg;
             const Trav<KT> t = j < cached ? st[j] : trav[j];
             const K kc = c == 0 ? key[0] : (c == 1 ? key[1] : key[D - 1]);
-            const bool left = (t.flags & TRAV_ALLLEFT) || KT::lt(kc, t.pivot);
+            bool left = (t.flags & TRAV_ALLLEFT) != 0;
+            if constexpr (KT::BAND) {
+                if (!left) {
+                    const int sd = band_side(kc, CutBounds{t.blo, t.bhi});
+                    left = sd < 0 || (sd == 0 && KeyF64::lt(band_code(bs, i, c == 0 ? 0 : (c == 1 ? 1 : D - 1)), t.pivot));
+                }
+            } else {
+                left = left || KT::lt(kc, t.pivot);
+            }
             if (L + 1 < levels)
                 seg = t.next + (left ? 0 : ((t.flags & TRAV_HAS_LEFT) ? 1 : 0));
             else
@@ -1265,7 +1583,8 @@ constexpr uint32_t TRAV_NX_ALLLEFT = 1u << 30, TRAV_NX_HASLEFT = 1u << 31, TRAV_
 
 template <class KT>
 __host__ __device__ constexpr size_t trav_smem_bytes(uint64_t total, uint64_t n_last) {
-    return n_last * sizeof(uint64_t) + total * (sizeof(typename KT::T) + sizeof(uint32_t));
+    return n_last * sizeof(uint64_t) +
+           total * (sizeof(typename KT::C) + sizeof(uint32_t) + (KT::BAND ? 2 * sizeof(float) : 0));
 }
 
 template <int D, class KT>
@@ -1274,18 +1593,22 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
                                                          const typename KT::T *__restrict__ k0,
                                                          const typename KT::T *__restrict__ k1,
                                                          const typename KT::T *__restrict__ k2, uint64_t n,
-                                                         uint64_t *__restrict__ part, const RunScalars *rs) {
+                                                         uint64_t *__restrict__ part, const RunScalars *rs,
+                                                         BandSrc bs) {
     typedef typename KT::T K;
+    typedef typename KT::C CK;
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ uint32_t s_off[MAX_TRAV_LEVELS];
     const uint32_t off_last = (uint32_t)lv.off[levels - 1];
-    uint64_t *s_heap = (uint64_t *)dsm;               // [total - off_last]
-    K *s_piv = (K *)(s_heap + (total - off_last));   // [total]
-    uint32_t *s_nx = (uint32_t *)(s_piv + total);     // [total]
+    uint64_t *s_heap = (uint64_t *)dsm;                       // [total - off_last]
+    CK *s_piv = (CK *)(s_heap + (total - off_last));          // [total]
+    float2 *s_bnd = (float2 *)(s_piv + total);                // band form: [total] (RD32, RU32)
+    uint32_t *s_nx = (uint32_t *)(s_bnd + (KT::BAND ? total : 0));  // [total]
     for (uint32_t j = threadIdx.x; j < total; j += BLOCK) {
         const Trav<KT> t = trav[j];
         const uint32_t fl = ((t.flags & TRAV_ALLLEFT) ? TRAV_NX_ALLLEFT : 0u) | ((t.flags & TRAV_HAS_LEFT) ? TRAV_NX_HASLEFT : 0u);
         s_piv[j] = t.pivot;
+        if constexpr (KT::BAND) s_bnd[j] = make_float2(t.blo, t.bhi);
         if (j < off_last) {
             s_nx[j] = fl | ((uint32_t)t.next & TRAV_NX_INDEX);
         } else {
@@ -1321,7 +1644,17 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
                 const uint32_t e = o + seg[k];
                 const uint32_t x = s_nx[e];
                 const K kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
-                const bool left = (x & TRAV_NX_ALLLEFT) || KT::lt(kc, s_piv[e]);
+                bool left = (x & TRAV_NX_ALLLEFT) != 0;
+                if constexpr (KT::BAND) {
+                    if (!left) {
+                        const float2 bd = s_bnd[e];
+                        const int sd = band_side(kc, CutBounds{bd.x, bd.y});
+                        const uint64_t i = base + (uint64_t)k * BLOCK;
+                        left = sd < 0 || (sd == 0 && i < n && KeyF64::lt(band_code(bs, i, c), s_piv[e]));
+                    }
+                } else {
+                    left = left || KT::lt(kc, s_piv[e]);
+                }
                 seg[k] = (x & TRAV_NX_INDEX) + ((!left && (x & TRAV_NX_HASLEFT)) ? 1u : 0u);
             }
             c = c + 1 == D ? 0 : c + 1;
@@ -1331,7 +1664,16 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
             const uint64_t i = base + (uint64_t)k * BLOCK;
             const uint32_t e = off_last + seg[k];
             const K kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
-            const bool left = (s_nx[e] & TRAV_NX_ALLLEFT) || KT::lt(kc, s_piv[e]);
+            bool left = (s_nx[e] & TRAV_NX_ALLLEFT) != 0;
+            if constexpr (KT::BAND) {
+                if (!left) {
+                    const float2 bd = s_bnd[e];
+                    const int sd = band_side(kc, CutBounds{bd.x, bd.y});
+                    left = sd < 0 || (sd == 0 && i < n && KeyF64::lt(band_code(bs, i, c), s_piv[e]));
+                }
+            } else {
+                left = left || KT::lt(kc, s_piv[e]);
+            }
             if (i < n) part[i] = 2 * s_heap[seg[k]] + (left ? 1 : 2) - hmin;
         }
     }
@@ -1344,7 +1686,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
 template <class KT>
 __global__ void __launch_bounds__(BLOCK) k_assign(const Seg<KT> *__restrict__ segs, uint32_t S, uint64_t n,
                                                   const typename KT::T *__restrict__ kc, const uint32_t *__restrict__ isrc,
-                                                  uint64_t *__restrict__ part, RunScalars *rs) {
+                                                  uint64_t *__restrict__ part, RunScalars *rs, BandSrc bs, int coord) {
     const uint64_t c0 = n * blockIdx.x / gridDim.x, c1 = n * (blockIdx.x + 1) / gridDim.x;
     if (c0 >= c1) return;
     const uint64_t hmin = rs->min_heap;
@@ -1354,8 +1696,15 @@ __global__ void __launch_bounds__(BLOCK) k_assign(const Seg<KT> *__restrict__ se
         const Seg<KT> sg = segs[k];
         const uint64_t pe = min(c1, sg.off + sg.n);
         const uint64_t hl = 2 * sg.heap + 1 - hmin, hr = 2 * sg.heap + 2 - hmin;
+        CutBounds pb = {0.f, 0.f};
+        if constexpr (KT::BAND) pb = band_bounds(sg.pivot);
         for (uint64_t e = pos + threadIdx.x; e < pe; e += BLOCK) {
-            const uint64_t id = goes_left<KT>(kc[e], sg) ? hl : hr;
+            bool left;
+            if constexpr (KT::BAND)
+                left = goes_left_band<KT>(kc[e], sg, pb, [&]() { return band_code(bs, isrc ? isrc[e] : e, coord); });
+            else
+                left = goes_left<KT>(kc[e], sg);
+            const uint64_t id = left ? hl : hr;
             const uint64_t dst = isrc ? isrc[e] : e;
             if (dst < n)
                 part[dst] = id;

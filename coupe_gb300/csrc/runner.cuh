@@ -63,12 +63,13 @@ struct Buffers {
     RunScalars *rs;
     uint64_t hist_bins;
 
-    size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap, bool index_path, uint64_t tcap) {
+    size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap, bool index_path, bool carry,
+                 uint64_t tcap) {
         for (int k = 0; k < 3; ++k)
             for (int d = 0; d < 3; ++d) keys[k][d] = d < D ? b.take<K>(n) : nullptr;
         for (int s = 0; s < 2; ++s) {
             w[s] = b.take<typename WT::S>(n);
-            idx[s] = index_path ? b.take<uint32_t>(n) : nullptr;
+            idx[s] = carry ? b.take<uint32_t>(n) : nullptr;
             segs[s] = b.take<Seg<KT>>(scap);
             list[s] = b.take<uint32_t>(scap);
             P[s] = b.take<uint64_t>(scap + 1);
@@ -94,7 +95,9 @@ static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem
 // What the set-up of a run hands to its level loop.
 struct RunSetup {
     uint64_t n = 0, iters = 0, lbcap = 0, bytes = 0;
-    bool index_path = false;
+    bool index_path = false;  // part ids from the segments (k_assign), not a traversal
+    bool carry = false;       // reorders carry input indices (index path, band form)
+    Mat M;                    // the basis change k_convert applied
     cudaStream_t s = nullptr;
     RunScalars *h_rs = nullptr;
     int g_stream = 0;
@@ -109,18 +112,19 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     typedef typename WL::S WS;
     const Tuning &tu = tuning();
     const uint64_t n = R0.n, iters = R0.iters;
-    const bool index_path = R0.index_path;
+    const bool index_path = R0.index_path, carry = R0.carry;
     cudaStream_t s = R0.s;
+    const BandSrc bs = make_band_src(a.d_points, R0.M, D, &B.rs->band_points);
     RunScalars *h_rs = R0.h_rs;
     const int g_stream = R0.g_stream;
     uint64_t bytes = R0.bytes;
     const int nbk_max = std::min(hist_max_nbk<WL>(), std::max(1, tu.max_nbk));
-    const size_t r_smem = reorder_smem<D, KT, WL>(index_path);
+    const size_t r_smem = reorder_smem<D, KT, WL>(carry);
     CG_CK(cudaFuncSetAttribute((const void *)k_traverse_smem<D, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)TRAV_SMEM_MAX));
-    CG_CK(cudaFuncSetAttribute((const void *)k_reorder<D, KT, WL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)r_smem));
-    const int g_reorder = occupancy_grid((const void *)k_reorder<D, KT, WL>, C.sms, BLOCK, r_smem);
+    const void *reorder_fn = carry ? (const void *)k_reorder<D, KT, WL, true> : (const void *)k_reorder<D, KT, WL, false>;
+    CG_CK(cudaFuncSetAttribute(reorder_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem));
+    const int g_reorder = occupancy_grid(reorder_fn, C.sms, BLOCK, r_smem);
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
     uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
     chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
@@ -131,7 +135,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     }
     const int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
     CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
-    const uint64_t sk = sizeof(K), sw = sizeof(WS), si = index_path ? 4 : 0;
+    const uint64_t sk = sizeof(K), sw = sizeof(WS), si = carry ? 4 : 0;
 
     int kb = 0;          // key buffer of the current level
     int sb = 0;          // segment table / weight buffer of the current level
@@ -163,6 +167,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             trav_l = B.trav + trav_used;
             trav_used += S;
         }
+        // band form: the items' input indices, for coordinates in the band
+        const uint32_t *hsrc = KT::BAND ? ic : nullptr;
         auto children = [&]() {
             CG_LAUNCH(KID_CHILDREN, 0,
                       k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
@@ -178,7 +184,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
         CG_LAUNCH(KID_HIST, n * (sk + sw),
                   k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], (uint32_t)S, kc, wc, H, nbk, n,
-                                                          B.rs, 0));
+                                                          B.rs, 0, hsrc, bs, coord, segs));
         ++st->hist_passes;
         st->hist_points += n;
         bytes += n * (sk + sw);
@@ -191,7 +197,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         // long it is: its kernels read the count the scan left and return at
         // once when no segment is searching.  The next scan leaves list[0].
         CG_LAUNCH(KID_HIST, 0,
-                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1));
+                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1, hsrc,
+                                                          bs, coord, segs));
         ++st->hist_passes;
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
@@ -212,12 +219,17 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         // rare: splits that need more steps than two passes replay
         int li = 0;
         bool more = false;
+        int extra = 0;
         while (h_rs->nactive > 0) {
             more = true;
+            if (++extra > 4096) {
+                *err = "a split did not finish after 4096 passes";
+                return COUPE_ERR_CRASH;
+            }
             const uint64_t nlist = h_rs->nactive;
             CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
                       k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs, 0));
+                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs));
             ++st->hist_passes;
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
@@ -249,7 +261,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         if (last) {
             if (index_path) {
                 CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
-                          k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs));
+                          k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs, bs,
+                                                                  coord));
                 bytes += n * (sk + (ic ? 4 : 0) + 8);
             } else {
                 const uint64_t n_last = trav_used - lv.off[iters - 1];
@@ -258,12 +271,12 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                     CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                               k_traverse_smem<D, KT><<<g_stream, BLOCK, tsm, s>>>(
                                   B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
-                                  B.keys[0][2], n, a.d_part, B.rs));
+                                  B.keys[0][2], n, a.d_part, B.rs, bs));
                 } else {
                     CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                               k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters,
                                                                            B.keys[0][0], B.keys[0][1], B.keys[0][2],
-                                                                           n, a.d_part, B.rs));
+                                                                           n, a.d_part, B.rs, bs));
                 }
                 bytes += n * (D * sk + 8);
             }
@@ -288,12 +301,17 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         R.wsrc = wc;
         R.wdst = (WS *)B.w[snext];
         R.isrc = ic;
-        R.idst = index_path ? B.idx[snext] : nullptr;
+        R.idst = carry ? B.idx[snext] : nullptr;
+        R.bs = bs;
         R.lb = B.lb;
         R.rs = B.rs;
         const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
-        CG_LAUNCH(KID_REORDER, rbytes,
-                  k_reorder<D, KT, WL><<<(unsigned)std::min<uint64_t>(g_reorder, nchunks), BLOCK, r_smem, s>>>(R));
+        const unsigned r_grid = (unsigned)std::min<uint64_t>(g_reorder, nchunks);
+        if (carry) {
+            CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, true><<<r_grid, BLOCK, r_smem, s>>>(R));
+        } else {
+            CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, false><<<r_grid, BLOCK, r_smem, s>>>(R));
+        }
         bytes += n * sk /* flag pre-count */ + rbytes;
         kb = kb_next;
         sb = snext;
@@ -321,6 +339,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     st->hist_points += h_rs->pass_points;
     bytes += h_rs->pass_points * (sk + sw);
     st->algo_bytes = bytes;
+    st->band_points = h_rs->band_points;
     if (h_rs->err) {
         uint32_t e = h_rs->err;
         if (e & ERR_NONFINITE_WEIGHT) {
@@ -372,11 +391,12 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
 
     Buffers<D, KT, WT> B;
     Bump dry{nullptr, 0};
-    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, tcap);
+    const bool carry = index_path || KT::BAND;
+    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap);
     int rc = ensure_workspace(C, need, err);
     if (rc != COUPE_ERR_OK) return rc;
     Bump real{(char *)C.ws, 0};
-    B.carve(real, n, scap, hb, lbcap, index_path, tcap);
+    B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap);
     RunScalars *h_rs = (RunScalars *)C.h_pinned;
 
     const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
@@ -414,6 +434,8 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     R0.n = n;
     R0.iters = a.iter_count;
     R0.index_path = index_path;
+    R0.carry = carry;
+    R0.M = M;
     R0.s = s;
     R0.h_rs = h_rs;
     R0.g_stream = g_stream;

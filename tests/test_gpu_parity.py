@@ -19,7 +19,8 @@ def _gpu(coupe, pts, w, iters, tol, mode="ref32", rib=False):
 
 
 def _oracle_mode(mode):
-    return 1 if mode == "f64" else 0
+    # the band form decides exactly like the F64 form
+    return 1 if mode in ("f64", "f32key_f64band") else 0
 
 
 # ---------------------------------------------------------------------------
@@ -98,7 +99,7 @@ def _make(n, dim, wk, seed):
     return pts, w
 
 
-@pytest.mark.parametrize("mode", ["ref32", "f64"])
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
 @pytest.mark.parametrize("n,dim,wk,iters,tol,seed", CASES)
 def test_parity_random(coupe, oracle_mod, n, dim, wk, iters, tol, seed, mode):
     pts, w = _make(n, dim, wk, seed)
@@ -133,14 +134,14 @@ def _check(coupe, oracle_mod, pts, w, iters, tol, mode="ref32", fsum=None, nan_r
     return got, st
 
 
-@pytest.mark.parametrize("mode", ["ref32", "f64"])
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
 def test_gaussian_clusters(coupe, oracle_mod, mode):
     from coupe_gb300 import workloads
     pts, w, cfg = workloads.gaussian_mixture3d(n=400_000, seed=3)
     _check(coupe, oracle_mod, pts, w, cfg["iter_count"], cfg["tolerance"], mode)
 
 
-@pytest.mark.parametrize("mode", ["ref32", "f64"])
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
 def test_planes_f64_weights(coupe, oracle_mod, mode):
     from coupe_gb300 import workloads
     pts, w, cfg = workloads.planes3d_lognormal(n=300_000, seed=4)
@@ -163,7 +164,7 @@ def test_special_values(coupe, oracle_mod):
     pts[3::59, 0] = 1e300   # beyond f32: key becomes inf in REF32
     pts[11::61, 1] = 1e-310  # subnormal f64
     w = rng.integers(1, 5, size=len(pts), dtype=np.int64)
-    for mode in ("ref32", "f64"):
+    for mode in ("ref32", "f64", "f32key_f64band"):
         _check(coupe, oracle_mod, pts, w, 7, 0.02, mode)
     # finite bounding box: signed zeros and subnormals
     pts = rng.standard_normal((20000, 2))
@@ -171,7 +172,7 @@ def test_special_values(coupe, oracle_mod):
     pts[::57, 1] = 0.0
     pts[11::61, 1] = 1e-310
     pts[13::67, 0] = -1e-40  # a subnormal f32 key
-    for mode in ("ref32", "f64"):
+    for mode in ("ref32", "f64", "f32key_f64band"):
         got, _ = _check(coupe, oracle_mod, pts, w, 7, 0.02, mode)
         assert len(set(got.tolist())) > 64
 
@@ -185,7 +186,7 @@ def test_nan_coordinates(coupe, oracle_mod):
     pts[7::89, 0] = np.nan
     pts[3::97, 1] = np.nan
     w = rng.integers(1, 5, size=len(pts), dtype=np.int64)
-    for mode in ("ref32", "f64"):
+    for mode in ("f32key_f64band", "f64", "ref32"):
         got, _ = _check(coupe, oracle_mod, pts, w, 7, 0.02, mode, nan_right=True)
     ref, _ = oracle_mod.rcb(pts, w, 7, 0.02)
     finite = np.isfinite(pts).all(axis=1)
@@ -210,7 +211,7 @@ def test_int32_wraparound(coupe, oracle_mod):
     _check(coupe, oracle_mod, pts, w, 6, 0.05)
 
 
-@pytest.mark.parametrize("mode", ["ref32", "f64"])
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
 def test_16bit_weight_copy_boundary(coupe, oracle_mod, mode):
     """Integer weights in [0, 2^16) run the level loop on a 16-bit copy: the
     largest such weight, one past it, odd segment offsets, and c_int sums that
@@ -298,7 +299,7 @@ def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     try:
         for k, v in knobs.items():
             coupe.set_option(k, v)
-        for mode, om in (("ref32", 0), ("f64", 1)):
+        for mode, om in (("ref32", 0), ("f64", 1), ("f32key_f64band", 1)):
             want, _ = oracle_mod.rcb(pts, w, 9, 0.01, mode=om)
             got = _gpu(coupe, pts, w, 9, 0.01, mode=mode)
             assert (want == got).all()
@@ -311,7 +312,7 @@ def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
             coupe.set_option(k, v)
 
 
-@pytest.mark.parametrize("mode", ["ref32", "f64"])
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
 def test_full_size_repeatable(coupe, oracle_mod, mode):
     """16.8 M points, 1024 parts (the benchmark workload): equal to the
     oracle once, then 40 device-resident runs in a row give the same ids and
@@ -331,6 +332,34 @@ def test_full_size_repeatable(coupe, oracle_mod, mode):
         part.fill_(-1)
         coupe.rcb_device(part, dp, dw, 10, 0.01, mode=mode)
         assert torch.equal(part, first)
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_band_inside_one_f32_interval(coupe, oracle_mod, dim):
+    """Band form: coordinates packed inside one or two f32 rounding intervals,
+    so that every cut of the first axis lies in the band: the f64 coordinate
+    decides every bin, every side and the exact minima of the stop test.  The
+    ids equal the F64 form's (the oracle's f64 mode)."""
+    rng = np.random.default_rng(31 + dim)
+    n = 60_000
+    pts = rng.random((n, dim))
+    pts[:, 0] = 1.0 + rng.integers(0, 1 << 21, size=n) * 2.0 ** -44  # within 2^-23 of 1
+    pts[::97, 0] = 1.0 + 2.0 ** -24  # the halfway point between two floats
+    w = rng.integers(1, 50, size=n, dtype=np.int64)
+    for iters, tol in ((6, 0.01), (9, 0.001)):
+        _check(coupe, oracle_mod, pts, w, iters, tol, "f32key_f64band")
+    st = coupe.last_stats()
+    assert st["mode"] == 2
+
+
+def test_rib_band_equals_f64(coupe):
+    """Rib in the band form gathers the rotated f64 coordinate exactly as the
+    conversion computed it: the ids equal the F64 form's."""
+    from coupe_gb300 import workloads
+    pts, w, _ = workloads.hex_mesh_rib(side=40, seed=8)
+    a = _gpu(coupe, pts, w, 9, 0.01, mode="f64", rib=True)
+    b = _gpu(coupe, pts, w, 9, 0.01, mode="f32key_f64band", rib=True)
+    assert (a == b).all()
 
 
 def test_key_conversion_is_ieee_rne(coupe):
