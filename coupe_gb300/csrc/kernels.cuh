@@ -1254,6 +1254,8 @@ __device__ __forceinline__ bool goes_left_band(float key, const Seg<KT> &sg, con
 struct TileRef {
     uint32_t kk;
     uint64_t ts, te;
+    uint64_t pend;  // end of the tile's piece (its segment, cut at the chunk end)
+    bool first;     // the tile starts its piece
     bool valid;
 };
 
@@ -1332,7 +1334,9 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         TileRef cur;
         cur.kk = kf;
         cur.ts = c0;
-        cur.te = min(cur.ts + R_TILE, piece_end(kf));
+        cur.pend = piece_end(kf);
+        cur.te = min(cur.ts + R_TILE, cur.pend);
+        cur.first = true;
         cur.valid = true;
         prefetch(cur, 0);  // overlaps the count below
         uint32_t ixn[R_ITEMS];  // indices of the next tile to process
@@ -1395,25 +1399,35 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             continue;
         }
         const uint64_t prefix_first = s_prefix;
-        Seg<KT> sg;
-        CutBounds pb = {0.f, 0.f};  // band form: bounds of sg.pivot
+        // the current piece's segment, as scalars (kept in registers rather
+        // than re-read from the segment table)
+        uint64_t p_off = 0, p_nleft = 0;
+        uint32_t p_state = 0;
+        typename KT::C p_pivot = 0;
+        CutBounds pb = {0.f, 0.f};  // band form: bounds of p_pivot
         uint64_t running = 0, seg_end = 0, left_end = 0;
         int tile_no = 0;
         while (cur.valid) {
-            // the next tile of the chunk (it may start the next segment)
+            // the next tile of the chunk (it may start the next segment); the
+            // segment table is read once per piece, here
             TileRef nxt;
             nxt.valid = false;
-            if (cur.te < piece_end(cur.kk)) {
+            if (cur.te < cur.pend) {
                 nxt.kk = cur.kk;
                 nxt.ts = cur.te;
+                nxt.pend = cur.pend;
+                nxt.first = false;
                 nxt.valid = true;
             } else if (cur.kk < kl) {
                 nxt.kk = cur.kk + 1;
-                nxt.ts = A.segs[nxt.kk].off;
+                const Seg<KT> &g = A.segs[nxt.kk];
+                nxt.ts = g.off;
+                nxt.pend = min(c1, g.off + g.n);
+                nxt.first = true;
                 nxt.valid = true;
             }
             if (nxt.valid) {
-                nxt.te = min(nxt.ts + R_TILE, piece_end(nxt.kk));
+                nxt.te = min(nxt.ts + R_TILE, nxt.pend);
                 prefetch(nxt, (tile_no + 1) & 1);
                 cp_async_wait<1>();
             } else {
@@ -1421,12 +1435,16 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             }
             __syncthreads();  // this tile's copies are visible to every thread
             const int buf = tile_no & 1;
-            if (tile_no == 0 || cur.ts == A.segs[cur.kk].off) {
-                sg = A.segs[cur.kk];
-                if constexpr (KT::BAND) pb = band_bounds(sg.pivot);
+            if (cur.first) {
+                const Seg<KT> &g = A.segs[cur.kk];
+                p_off = g.off;
+                p_nleft = g.nleft;
+                p_state = g.state;
+                p_pivot = g.pivot;
+                if constexpr (KT::BAND) pb = band_bounds(p_pivot);
                 running = cur.kk == kf ? prefix_first : 0;
-                seg_end = sg.off + sg.n;
-                left_end = sg.off + sg.nleft;
+                seg_end = p_off + g.n;
+                left_end = p_off + p_nleft;
             }
             const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
             const K *tkc = tile_keys(buf, A.coord);
@@ -1443,11 +1461,11 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             for (int i = 0; i < R_ITEMS; ++i) {
                 const uint32_t li = i * BLOCK + threadIdx.x;
                 if constexpr (KT::BAND)
-                    fl[i] = li < tcount && goes_left_band<KT>(tkc[li], sg, pb, [&]() {
-                                return band_code(A.bs, ix[i], A.coord);
-                            });
+                    fl[i] = li < tcount &&
+                            (p_state == SEG_ALLLEFT || band_side(tkc[li], pb) < 0 ||
+                             (band_side(tkc[li], pb) == 0 && KeyF64::lt(band_code(A.bs, ix[i], A.coord), p_pivot)));
                 else
-                    fl[i] = li < tcount && goes_left<KT>(tkc[li], sg);
+                    fl[i] = li < tcount && (p_state == SEG_ALLLEFT || KT::lt(tkc[li], p_pivot));
                 bal[i] = __ballot_sync(0xffffffffu, fl[i]);
                 if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
             }
@@ -1494,8 +1512,8 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             }
             __syncthreads();
             // write the left run and the right run, coalesced
-            const uint64_t left_base = sg.off + running;
-            const uint64_t right_base = sg.off + sg.nleft + (cur.ts - sg.off - running);
+            const uint64_t left_base = p_off + running;
+            const uint64_t right_base = p_off + p_nleft + (cur.ts - p_off - running);
             for (uint32_t k = threadIdx.x; k < tcount; k += BLOCK) {
                 const uint32_t src = perm[k];
                 const uint64_t d = k < tile_left ? left_base + k : right_base + (k - tile_left);
