@@ -199,6 +199,11 @@ __device__ __forceinline__ uint64_t band_code(const BandSrc &bs, uint64_t orig, 
     atomicAdd(bs.count, 1ull);
     return KeyF64::from_f64(x);
 }
+// The same, out of line: for the rare band items of hot loops, so that the
+// loops stay small (fewer branches and instruction-cache misses).
+static __device__ __noinline__ uint64_t band_code_cold(const BandSrc *bs, uint64_t orig, int coord) {
+    return band_code(*bs, orig, coord);
+}
 
 // ---------------------------------------------------------------------------
 // k_convert: AoS f64 points -> D SoA key arrays (coupe's `point[coord] as
@@ -1345,15 +1350,26 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         const Seg<KT> sl = A.segs[kl];
         const uint64_t la = max(c0, sl.off);
         uint64_t cnt = 0;
-        if constexpr (KT::BAND) {
-            const CutBounds pb = band_bounds(sl.pivot);
-            for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK)
-                cnt += goes_left_band<KT>(kc[e], sl, pb,
-                                          [&]() { return band_code(A.bs, A.isrc ? A.isrc[e] : e, A.coord); })
-                           ? 1
-                           : 0;
-        } else {
-            for (uint64_t e = la + threadIdx.x; e < c1; e += BLOCK) cnt += goes_left<KT>(kc[e], sl) ? 1 : 0;
+        {
+            CutBounds spb = {0.f, 0.f};
+            if constexpr (KT::BAND) spb = band_bounds(sl.pivot);
+            auto left = [&](K k, uint64_t e) -> uint32_t {
+                if constexpr (KT::BAND) {
+                    if (sl.state == SEG_ALLLEFT) return 1u;
+                    const int sd = band_side(k, spb);
+                    if (sd != 0) return sd < 0 ? 1u : 0u;
+                    return KeyF64::lt(band_code_cold(&A.bs, A.isrc ? A.isrc[e] : e, A.coord), sl.pivot) ? 1u : 0u;
+                } else {
+                    return goes_left<KT>(k, sl) ? 1u : 0u;
+                }
+            };
+            // four loads in flight per thread
+            uint64_t e = la + threadIdx.x;
+            for (; e + 3 * BLOCK < c1; e += 4 * BLOCK) {
+                const K k0 = kc[e], k1 = kc[e + BLOCK], k2 = kc[e + 2 * BLOCK], k3 = kc[e + 3 * BLOCK];
+                cnt += left(k0, e) + left(k1, e + BLOCK) + left(k2, e + 2 * BLOCK) + left(k3, e + 3 * BLOCK);
+            }
+            for (; e < c1; e += BLOCK) cnt += left(kc[e], e);
         }
         uint64_t agg;
         block_exscan_u64(cnt, sh, agg);
@@ -1463,7 +1479,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
                 if constexpr (KT::BAND)
                     fl[i] = li < tcount &&
                             (p_state == SEG_ALLLEFT || band_side(tkc[li], pb) < 0 ||
-                             (band_side(tkc[li], pb) == 0 && KeyF64::lt(band_code(A.bs, ix[i], A.coord), p_pivot)));
+                             (band_side(tkc[li], pb) == 0 && KeyF64::lt(band_code_cold(&A.bs, ix[i], A.coord), p_pivot)));
                 else
                     fl[i] = li < tcount && (p_state == SEG_ALLLEFT || KT::lt(tkc[li], p_pivot));
                 bal[i] = __ballot_sync(0xffffffffu, fl[i]);
