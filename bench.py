@@ -253,7 +253,7 @@ def main():
     top = max(prof.items(), key=lambda kv: kv[1]["ms"])
     peak, peak_kind = measured_peak()
     achieved = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9
-    traffic = _traffic_per_launch(top[0])
+    traffic = _traffic_per_launch(top[0], headline)
     roofline = {"bound": "hbm", "kernel": top[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": top[1]["bytes"] // max(1, top[1]["launches"]),
@@ -335,12 +335,13 @@ def _mode_available(coupe, pts, w, part):
         return False
 
 
-def _traffic_per_launch(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+def _traffic_per_launch(kernel, mode):
+    """DRAM bytes per launch of `kernel` in `mode` from the committed ncu summary."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
-            return json.load(f).get(kernel)
+            t = json.load(f)
+        return t.get("%s:%s" % (mode, kernel), t.get(kernel))
     except Exception:
         return None
 

@@ -549,7 +549,7 @@ __host__ __device__ constexpr int hist_max_nbk() {
 // shared-memory histogram flushed to the segment's global bins.
 // ---------------------------------------------------------------------------
 template <class KT, class WT>
-__global__ void __launch_bounds__(BLOCK, 4) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+__global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
