@@ -19,7 +19,7 @@ import numpy as np
 
 __all__ = [
     "Rcb", "Rib", "CoupeError", "lib", "library_path", "MODES", "last_stats",
-    "rcb_device", "rib_device", "rib_matrix_device",
+    "rcb_device", "rib_device", "rib_matrix_device", "rcb_batched_device",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -39,7 +39,7 @@ EXPORTED = [
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
-    "coupe_gpu_split_noalloc",
+    "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched",
 ]
 
 
@@ -97,6 +97,8 @@ def lib():
     L.coupe_gpu_rcb_device.restype = i32
     L.coupe_gpu_rib_device.argtypes = [vp, u64, u64, vp, i32, vp, u64, dbl, i32, vp]
     L.coupe_gpu_rib_device.restype = i32
+    L.coupe_gpu_rcb_batched.argtypes = [vp, u64, vp, u64, vp, i32, vp, vp, dbl, i32, vp]
+    L.coupe_gpu_rcb_batched.restype = i32
     L.coupe_gpu_rib_matrix.argtypes = [u64, u64, vp, vp, vp]
     L.coupe_gpu_rib_matrix.restype = i32
     L.coupe_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
@@ -248,6 +250,27 @@ def rcb_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", m
     rc = lib().coupe_gpu_rcb_device(_ptr(part_ids), n, dim, _ptr(points), wt, _ptr(weights), iter_count,
                                     tolerance, MODES[mode], m.ctypes.data if m is not None else None,
                                     ctypes.c_void_p(s))
+    _check(rc)
+
+
+def rcb_batched_device(part_ids, points, weights, set_offsets, iter_counts, tolerance, mode="ref32", stream=None):
+    """Rcb of several independent point sets in one run, on CUDA tensors:
+    set k is rows set_offsets[k]:set_offsets[k + 1] of points (N, D) float64,
+    weights (N,) and part_ids (N,), split into at most 2**iter_counts[k]
+    parts with ids from 0, as a separate rcb_device call on that set gives.
+    set_offsets (nsets + 1) and iter_counts (nsets) are host sequences."""
+    import torch
+    n, dim = points.shape
+    wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+    off = np.ascontiguousarray(np.asarray(set_offsets, dtype=np.uint64))
+    it = np.ascontiguousarray(np.asarray(iter_counts, dtype=np.uint32))
+    if off.ndim != 1 or it.ndim != 1 or len(off) != len(it) + 1:
+        raise ValueError("set_offsets needs one entry more than iter_counts")
+    if len(it) and int(off[-1]) != n:
+        raise CoupeError(ERR_LEN_MISMATCH, "the last set offset must equal the number of points")
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_rcb_batched(_ptr(part_ids), len(it), off.ctypes.data, dim, _ptr(points), wt,
+                                     _ptr(weights), it.ctypes.data, tolerance, MODES[mode], ctypes.c_void_p(s))
     _check(rc)
 
 

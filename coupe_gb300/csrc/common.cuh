@@ -448,6 +448,7 @@ template <class KT>
 struct Seg {
     typedef typename KT::C K;
     uint64_t off;    // first item
+    uint64_t voff;   // first item in the level's list of items still being split (off, when none has left)
     uint64_t heap;   // heap id: children of h are 2h+1 and 2h+2 (wrapping)
     uint64_t sum;    // weight sum (V bits)
     uint64_t prev;   // prev_count_left of the split loop (UINT64_MAX first)
@@ -459,7 +460,7 @@ struct Seg {
     uint32_t child;  // index of the first non-empty child in the next level
     uint32_t xstate; // band form: X_PENDING when xmin holds an exact minimum
     uint32_t xkey;   // band form: the f32 key (ordered) whose exact minimum xmin is
-    uint32_t pad;
+    uint32_t set;    // point set of the run the segment belongs to
     uint64_t xcut;   // band form: ... among the items at or right of this cut
     uint64_t xmin;   // band form: that minimum (f64 ordered code)
     K lo, hi;        // current search interval on this level's axis
@@ -485,6 +486,21 @@ struct Trav {
 constexpr int MAX_TRAV_LEVELS = 63;
 struct LevelOffsets {
     uint64_t off[MAX_TRAV_LEVELS];
+};
+
+// The point sets of a run: independent Rcb problems over consecutive item
+// ranges of the input, each with its own iteration count.  One set: its
+// totals live in RunScalars and these arrays are not read.
+struct SetTab {
+    uint32_t count;
+    const uint64_t *off;    // [count + 1] first item of each set, input order
+    const uint32_t *iters;  // [count] the set's iter_count
+    const uint32_t *root;   // [count] index of the set's root segment on level 0 (~0u: none)
+    uint64_t *bmin, *bmax;  // [count * 3] bounding box, ordered f64 codes
+    uint64_t *wsum;         // [count * 4] weight sum limbs
+    uint64_t *wabs;         // [count] largest |w| as raw f64 bits (f64 weights)
+    int32_t *fs;            // [count] fixed-point scale (f64 weights)
+    uint64_t *minheap;      // [count] smallest heap id among the set's parts
 };
 
 // Error bits raised by kernels (read by the host after each synchronisation).
@@ -519,6 +535,7 @@ struct RunScalars {
     uint32_t nexact;       // band form: decisions that waited for an exact minimum
     uint32_t pad2;
     unsigned long long band_points;  // band form: f64 coordinates read
+    uint64_t items_next;             // items of the next level's segments
 };
 
 }  // namespace cg

@@ -26,6 +26,12 @@ struct RunArgs {
     bool has_matrix = false;
     double matrix[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // row-major dim x dim
     cudaStream_t stream = nullptr;
+    // several independent point sets (nsets > 1): set k is items
+    // [set_off[k], set_off[k + 1]) with iter_count set_iters[k]; host arrays.
+    // iter_count is then unused.
+    uint64_t nsets = 1;
+    const uint64_t *set_off = nullptr;
+    const uint32_t *set_iters = nullptr;
 };
 
 // Process-wide tuning knobs (coupe_gpu_set_option).  They change how the

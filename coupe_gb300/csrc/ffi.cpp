@@ -328,6 +328,66 @@ enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t 
                        nullptr, stream);
 }
 
+enum coupe_err coupe_gpu_rcb_batched(uint64_t *d_partition, uint64_t nsets, const uint64_t *set_offsets,
+                                     uint64_t dimension, const double *d_points, enum coupe_type weight_type,
+                                     const void *d_weights, const uint32_t *iter_counts, double tolerance, int mode,
+                                     void *stream) {
+    t_err.clear();
+    std::memset(&t_stats, 0, sizeof(t_stats));
+    t_stats.mode = mode;
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (weight_type < COUPE_INT || weight_type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (nsets == 0) return COUPE_ERR_OK;
+    if (!set_offsets || !iter_counts) {
+        t_err = "set offsets and iteration counts are required";
+        return COUPE_ERR_LEN_MISMATCH;
+    }
+    if (nsets >= (1ull << 31)) {
+        t_err = "more than 2^31 - 1 sets";
+        return COUPE_ERR_ALLOC;
+    }
+    if (set_offsets[0] != 0) {
+        t_err = "set offsets must start at 0";
+        return COUPE_ERR_LEN_MISMATCH;
+    }
+    for (uint64_t k = 0; k < nsets; ++k)
+        if (set_offsets[k + 1] < set_offsets[k]) {
+            t_err = "set offsets must not decrease";
+            return COUPE_ERR_LEN_MISMATCH;
+        }
+    const uint64_t n = set_offsets[nsets];
+    if (n == 0) return COUPE_ERR_OK;
+    if (nsets == 1)
+        return device_call(false, d_partition, n, dimension, d_points, weight_type, d_weights, iter_counts[0],
+                           tolerance, mode, nullptr, stream);
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    cg::RunArgs a;
+    a.n = n;
+    a.dim = (int)dimension;
+    a.d_points = d_points;
+    a.wtype = weight_type;
+    a.d_weights = d_weights;
+    a.d_part = d_partition;
+    a.tolerance = tolerance;
+    a.mode = mode;
+    a.stream = (cudaStream_t)stream;
+    a.nsets = nsets;
+    a.set_off = set_offsets;
+    a.set_iters = iter_counts;
+    int rc = cg::run_rcb(*C, a, &t_stats, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
 enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double *d_points, double *obb_to_aabb,
                                     void *stream) {
     t_err.clear();

@@ -127,6 +127,43 @@ __device__ __forceinline__ uint32_t seg_index_of(const Seg<KT> *segs, uint32_t S
     }
     return lo;
 }
+// The same by position in the level's list of items (Seg::voff).
+template <class KT>
+__device__ __forceinline__ uint32_t seg_index_of_v(const Seg<KT> *segs, uint32_t S, uint64_t x) {
+    uint32_t lo = 0, hi = S;
+    while (hi - lo > 1) {
+        uint32_t m = (lo + hi) >> 1;
+        if (segs[m].voff <= x)
+            lo = m;
+        else
+            hi = m;
+    }
+    return lo;
+}
+
+// The set of input item i, remembered across calls: a thread walking items in
+// increasing order searches the set table only when it leaves the last set.
+struct SetCursor {
+    uint32_t s = ~0u;
+    uint64_t beg = 1, end = 0;
+    // true when i is in another set than the previous item
+    __device__ __forceinline__ bool move(const SetTab &T, uint64_t i) {
+        if (i >= beg && i < end) return false;
+        s = upper_index(T.off, T.count + 1, i);  // the last set starting at or before i
+        beg = T.off[s];
+        end = T.off[s + 1];
+        return true;
+    }
+};
+
+// Items [c0, c1) of n for CTA b of g when a CTA walks one contiguous range
+// (tiles of `tile` items), so that its items span few sets.
+struct CtaRange {
+    uint64_t t0, t1;  // tiles
+};
+__device__ __forceinline__ CtaRange cta_tiles(uint64_t ntiles, uint32_t b, uint32_t g) {
+    return CtaRange{ntiles * b / g, ntiles * (b + 1) / g};
+}
 
 __device__ __forceinline__ void atomic_max_ord(uint32_t *p, uint32_t v) { atomicMax(p, v); }
 __device__ __forceinline__ void atomic_max_ord(uint64_t *p, uint64_t v) {
@@ -210,13 +247,13 @@ static __device__ __noinline__ uint64_t band_code_cold(const BandSrc *bs, uint64
 // f32`, recursive_bisection.rs:674-679), optionally after the Rib basis change
 // p' = M p accumulated column by column (geometry.rs:203-205), and the f64
 // bounding box (BoundingBox::from_points, geometry.rs:33-78: NaN never
-// updates, the fold starts at f64::MAX / f64::MIN).
+// updates, the fold starts at f64::MAX / f64::MIN), per point set.
 // ---------------------------------------------------------------------------
 template <int D, class KT>
 __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pts, uint64_t n, Mat M,
                                                    typename KT::T *__restrict__ k0,
                                                    typename KT::T *__restrict__ k1,
-                                                   typename KT::T *__restrict__ k2, RunScalars *rs) {
+                                                   typename KT::T *__restrict__ k2, RunScalars *rs, SetTab sets) {
     typedef typename KT::T K;
     __shared__ uint64_t red[2 * 3][NWARPS];
     uint64_t mn[3], mx[3];
@@ -226,6 +263,21 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         mx[d] = ord_f64(-1.7976931348623157e308);
     }
     K *outs[3] = {k0, k1, k2};
+    // Several sets: each CTA converts one contiguous range of tiles and each
+    // thread sends its box to the set table whenever its items enter another
+    // set (a few times per thread).
+    const bool multi = sets.count > 1;
+    SetCursor cur;
+    auto flush = [&]() {
+        if (cur.s == ~0u) return;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            atomicMin((unsigned long long *)&sets.bmin[cur.s * 3 + d], (unsigned long long)mn[d]);
+            atomicMax((unsigned long long *)&sets.bmax[cur.s * 3 + d], (unsigned long long)mx[d]);
+            mn[d] = ord_f64(1.7976931348623157e308);
+            mx[d] = ord_f64(-1.7976931348623157e308);
+        }
+    };
     // q receives the raw bits of the (mapped) coordinates; without a basis
     // change nothing here executes an f64 instruction
     auto point = [&](const double *p, uint64_t *q) {
@@ -271,10 +323,17 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         cp_async_commit();
     };
     int buf = 0;
-    if ((uint64_t)blockIdx.x < ntiles) prefetch(blockIdx.x, 0);
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const uint64_t tn = t + gridDim.x;
-        if (tn < ntiles) {
+    uint64_t t_first = blockIdx.x, t_end = ntiles, t_step = gridDim.x;
+    if (multi) {
+        const CtaRange r = cta_tiles(ntiles, blockIdx.x, gridDim.x);
+        t_first = r.t0;
+        t_end = r.t1;
+        t_step = 1;
+    }
+    if (t_first < t_end) prefetch(t_first, 0);
+    for (uint64_t t = t_first; t < t_end; t += t_step) {
+        const uint64_t tn = t + t_step;
+        if (tn < t_end) {
             prefetch(tn, buf ^ 1);
             cp_async_wait<1>();
         } else {
@@ -287,6 +346,10 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         for (int r = 0; r < CONV_TILE / BLOCK; ++r) {
             const uint32_t j = r * BLOCK + threadIdx.x;
             if (j < np) {
+                if (multi && (p0 + j < cur.beg || p0 + j >= cur.end)) {
+                    flush();
+                    cur.move(sets, p0 + j);
+                }
                 uint64_t q[D];
                 point(&tile[buf][j * D], q);
 #pragma unroll
@@ -295,6 +358,10 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         }
         __syncthreads();  // the buffer is free for the tile after next
         buf ^= 1;
+    }
+    if (multi) {
+        flush();
+        return;
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -322,14 +389,42 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
 }
 
 // Largest |w| of f64 weights as raw bits (non-finite values sort above).
-static __global__ void __launch_bounds__(BLOCK) k_wabs_max(const double *__restrict__ w, uint64_t n, RunScalars *rs) {
+static __global__ void __launch_bounds__(BLOCK) k_wabs_max(const double *__restrict__ w, uint64_t n, RunScalars *rs,
+                                                          SetTab sets) {
     uint64_t m = 0;
+    if (sets.count > 1) {
+        // one contiguous range per CTA; a thread's maximum goes to its set
+        // whenever its items enter another set
+        const CtaRange r = cta_tiles((n + BLOCK - 1) / BLOCK, blockIdx.x, gridDim.x);
+        SetCursor cur;
+        for (uint64_t i = r.t0 * BLOCK + threadIdx.x; i < min(n, r.t1 * BLOCK); i += BLOCK) {
+            if (i < cur.beg || i >= cur.end) {
+                if (cur.s != ~0u) atomicMax((unsigned long long *)&sets.wabs[cur.s], (unsigned long long)m);
+                m = 0;
+                cur.move(sets, i);
+            }
+            const uint64_t b = (uint64_t)__double_as_longlong(w[i]) & 0x7fffffffffffffffull;
+            m = b > m ? b : m;
+        }
+        if (cur.s != ~0u) atomicMax((unsigned long long *)&sets.wabs[cur.s], (unsigned long long)m);
+        return;
+    }
     for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
         uint64_t b = (uint64_t)__double_as_longlong(w[i]) & 0x7fffffffffffffffull;
         m = b > m ? b : m;
     }
     m = warp_max_u64(m);
     if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&rs->wabs_max_bits, (unsigned long long)m);
+}
+
+// Several sets, f64 weights: each set's fixed-point scale (from its own
+// largest |w| and size, as a run of that set alone chooses it).
+static __global__ void k_set_fs(SetTab sets, RunScalars *rs) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= sets.count) return;
+    const uint64_t b = sets.wabs[s];
+    if (b >= 0x7ff0000000000000ull) atomicOr(&rs->err, ERR_NONFINITE_WEIGHT);
+    sets.fs[s] = fixed_scale_from_max(__longlong_as_double((long long)b), sets.off[s + 1] - sets.off[s]);
 }
 
 __device__ __forceinline__ int run_fscale(const RunScalars *rs, uint64_t n) {
@@ -339,13 +434,37 @@ __device__ __forceinline__ int run_fscale(const RunScalars *rs, uint64_t n) {
 // Total weight (recursive_bisection.rs:684), order independent.
 template <class WT>
 __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict__ w, uint64_t n, RunScalars *rs,
-                                                uint16_t *__restrict__ c16) {
-    const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
+                                                uint16_t *__restrict__ c16, SetTab sets) {
+    const bool multi = sets.count > 1;
+    int fs = WT::LIMBS > 1 && !multi ? run_fscale(rs, n) : 0;
     uint64_t acc[WT::LIMBS];
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) acc[l] = 0;
     bool wide = WT::LIMBS > 1, not16 = false;
-    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+    // several sets: one contiguous range per CTA; a thread's sum goes to its
+    // set whenever its items enter another set
+    uint64_t i0 = (uint64_t)blockIdx.x * BLOCK + threadIdx.x, i1 = n, step = (uint64_t)gridDim.x * BLOCK;
+    if (multi) {
+        const CtaRange r = cta_tiles((n + BLOCK - 1) / BLOCK, blockIdx.x, gridDim.x);
+        i0 = r.t0 * BLOCK + threadIdx.x;
+        i1 = min(n, r.t1 * BLOCK);
+        step = BLOCK;
+    }
+    SetCursor cur;
+    auto flush = [&]() {
+        if (cur.s == ~0u) return;
+#pragma unroll
+        for (int l = 0; l < WT::LIMBS; ++l) {
+            if (acc[l]) atomicAdd((unsigned long long *)&sets.wsum[cur.s * 4 + l], (unsigned long long)acc[l]);
+            acc[l] = 0;
+        }
+    };
+    for (uint64_t i = i0; i < i1; i += step) {
+        if (multi && (i < cur.beg || i >= cur.end)) {
+            flush();
+            cur.move(sets, i);
+            if (WT::LIMBS > 1) fs = sets.fs[cur.s];
+        }
         const typename WT::S wi = w[i];
         uint64_t q[WT::LIMBS];
         WT::limbs(wi, fs, q);
@@ -361,25 +480,28 @@ __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict
         }
     }
     if (__any_sync(0xffffffffu, not16) && (threadIdx.x & 31) == 0) atomicOr(&rs->narrow16, 1u);
+    if (__any_sync(0xffffffffu, wide) && (threadIdx.x & 31) == 0) atomicOr(&rs->wide, 1u);
+    if (multi) {
+        flush();
+        return;
+    }
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) {
         uint64_t v = warp_sum_u64(acc[l]);
         if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long *)&rs->wsum_limbs[l], (unsigned long long)v);
     }
-    if (__any_sync(0xffffffffu, wide) && (threadIdx.x & 31) == 0) atomicOr(&rs->wide, 1u);
 }
 
-// Root segment of level 0 (rcb_recurse's first call, recursive_bisection.rs:696).
+// A root segment: items [off, off + n), its weight sum and its f64 box
+// (rcb_recurse's first call, recursive_bisection.rs:696).
 template <class KT, class WT>
-__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs) {
-    typedef typename KT::T K;
-    const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
-    rs->fscale = fs;
-    if (WT::LIMBS > 1 && rs->wabs_max_bits >= 0x7ff0000000000000ull) rs->err |= ERR_NONFINITE_WEIGHT;
+__device__ Seg<KT> root_seg(uint64_t off, uint64_t voff, uint64_t n, uint32_t set, const uint64_t *limbs, int fs,
+                            const uint64_t *bmin, const uint64_t *bmax, int D) {
     Seg<KT> s;
-    s.off = 0;
+    s.off = off;
+    s.voff = voff;
     s.heap = 0;
-    s.sum = WT::bits(WT::value(rs->wsum_limbs, fs));
+    s.sum = WT::bits(WT::value(limbs, fs));
     s.prev = ~0ull;
     s.wl = 0;
     s.n = (uint32_t)n;
@@ -389,12 +511,12 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
     s.child = 0;
     s.xstate = 0;
     s.xkey = 0;
-    s.pad = 0;
+    s.set = set;
     s.xcut = 0;
     s.xmin = ~0ull;
     for (int d = 0; d < 3; ++d) {
-        double a = d < D ? unord_f64(rs->bbox_min_ord[d]) : 0.0;
-        double b = d < D ? unord_f64(rs->bbox_max_ord[d]) : 0.0;
+        double a = d < D ? unord_f64(bmin[d]) : 0.0;
+        double b = d < D ? unord_f64(bmax[d]) : 0.0;
         s.bmin[d] = KT::cut_from_f64(a);
         s.bmax[d] = KT::cut_from_f64(b);
     }
@@ -402,10 +524,47 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
     s.hi = s.bmax[0];
     s.pivot = 0;
     s.split_pos = 0;
-    segs[0] = s;
+    return s;
+}
+
+// Root segment of a one-set run.
+template <class KT, class WT>
+__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs) {
+    const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
+    rs->fscale = fs;
+    if (WT::LIMBS > 1 && rs->wabs_max_bits >= 0x7ff0000000000000ull) rs->err |= ERR_NONFINITE_WEIGHT;
+    segs[0] = root_seg<KT, WT>(0, 0, n, 0, rs->wsum_limbs, fs, rs->bbox_min_ord, rs->bbox_max_ord, D);
     list[0] = 0;
     P[0] = 0;
     P[1] = n;
+}
+
+// Root segments of several sets: root r belongs to set roots[r] and starts at
+// P[r] in the level's list of items (P written by the host).
+template <class KT, class WT>
+__global__ void k_roots(Seg<KT> *segs, uint32_t *list, const uint64_t *P, const uint32_t *roots, uint32_t nroots,
+                        int D, SetTab sets) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nroots) return;
+    const uint32_t st = roots[r];
+    const int fs = WT::LIMBS > 1 ? sets.fs[st] : 0;
+    segs[r] = root_seg<KT, WT>(sets.off[st], P[r], sets.off[st + 1] - sets.off[st], st, &sets.wsum[st * 4], fs,
+                               &sets.bmin[st * 3], &sets.bmax[st * 3], D);
+    list[r] = r;
+}
+
+// Initial values of the set table's accumulators.
+static __global__ void k_sets_init(SetTab sets) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= sets.count) return;
+    for (int d = 0; d < 3; ++d) {
+        sets.bmin[s * 3 + d] = ord_f64(1.7976931348623157e308);
+        sets.bmax[s * 3 + d] = ord_f64(-1.7976931348623157e308);
+    }
+    for (int l = 0; l < 4; ++l) sets.wsum[s * 4 + l] = 0;
+    sets.wabs[s] = 0;
+    sets.fs[s] = 0;
+    sets.minheap[s] = ~0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -555,7 +714,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
                                                 uint64_t n_total, const RunScalars *rs, int nlist_dev,
                                                 const uint32_t *__restrict__ isrc, BandSrc bs, int coord,
-                                                Seg<KT> *segs_w) {
+                                                Seg<KT> *segs_w, const int32_t *__restrict__ set_fs) {
     typedef typename KT::T K;
     typedef typename KT::C CK;
     typedef typename KT::Ord O;
@@ -568,7 +727,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     __shared__ uint32_t scnt[HNB];
     __shared__ O sinv[HNB];
     const int NB = 1 << nbk;
-    const int fs = L > 1 ? rs->fscale : 0;
+    int fs = L > 1 ? rs->fscale : 0;  // several sets: each set's own (set_fs)
     const bool packed = L == 1 && rs->wide == 0;
     if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass: the list the last scan left
     const uint64_t T = P[nlist];
@@ -581,6 +740,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         const uint32_t s = list[k];
         const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
         const Seg<KT> &sg = segs[s];
+        if (L > 1 && set_fs) fs = set_fs[sg.set];
         const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
         const CK lo = sg.lo, hi = sg.hi;
         __syncthreads();
@@ -810,7 +970,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
 template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
-                                                  RunScalars *rs, int nlist_dev) {
+                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs) {
     typedef typename KT::C K;  // cuts and interval bounds
     typedef typename KT::Ord O;
     typedef typename WT::V V;
@@ -828,7 +988,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     // whose halves span whole blocks use the block totals; once a half is
     // narrower than a block, the one block left is spread over the lanes.
     const int BS = NB >= 32 ? NB / 32 : 1;
-    const int fs = L > 1 ? rs->fscale : 0;
+    const int fs = L > 1 ? (set_fs ? set_fs[sg.set] : rs->fscale) : 0;
     const size_t g0 = (size_t)s * NB;
     auto load_bin = [&](int b, uint64_t &c, uint64_t *w, O &m) {
         const size_t g = g0 + b;
@@ -1099,21 +1259,23 @@ __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ 
 // dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
 // the smallest heap id among the children (the id offset, :698-702).
 template <class KT, class WT>
-__global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D,
-                                                   int write, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
-                                                   uint64_t n_total, Trav<KT> *trav, RunScalars *rs) {
+__global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
+                                                   uint32_t level, Seg<KT> *next, uint32_t *next_list,
+                                                   uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets) {
     typedef typename KT::T K;
     __shared__ uint64_t sh[33];
     // launched right after a speculative pass: nothing to do while a segment
     // of the level is still searching (the host runs more passes, then this)
     if (rs->nactive != 0) return;
-    uint64_t outc = 0;
+    const bool multi = sets.count > 1;
+    uint64_t outc = 0, outv = 0;
     uint64_t hmin = ~0ull;
     const int nc = (coord + 1) % D;
     for (uint32_t base = 0; base < S; base += blockDim.x) {
         const uint32_t s = base + threadIdx.x;
         Seg<KT> sg;
         uint32_t nl = 0, nr = 0;
+        bool leaves = !write;  // the children are parts: no segments for them
         if (s < S) {
             sg = segs[s];
             nl = sg.nleft;
@@ -1122,18 +1284,27 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                 nl = sg.n;
             }
             nr = sg.n - nl;
+            if (multi && sets.iters[sg.set] <= level + 1) leaves = true;  // the set's last level
         }
-        uint64_t tc;
-        const uint64_t ci = block_exscan_u64((nl > 0) + (nr > 0), sh, tc);
+        uint64_t tc, tv;
+        const uint64_t ci = block_exscan_u64(leaves ? 0 : (nl > 0) + (nr > 0), sh, tc);
+        const uint64_t vi = block_exscan_u64(leaves ? 0 : (uint64_t)nl + nr, sh, tv);
         if (s < S) {
             const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
-            if (nl > 0) hmin = hl < hmin ? hl : hmin;
-            if (nr > 0) hmin = hr < hmin ? hr : hmin;
+            if (leaves) {
+                uint64_t h = ~0ull;
+                if (nl > 0) h = hl;
+                if (nr > 0) h = hr < h ? hr : h;
+                if (multi)
+                    atomicMin((unsigned long long *)&sets.minheap[sg.set], (unsigned long long)h);
+                else
+                    hmin = h < hmin ? h : hmin;
+            }
             if (trav) {
                 Trav<KT> t;
                 t.pivot = sg.pivot;
                 t.flags = (sg.state == SEG_ALLLEFT ? TRAV_ALLLEFT : 0u) | (nl > 0 ? TRAV_HAS_LEFT : 0u);
-                t.next = write ? outc + ci : sg.heap;
+                t.next = leaves ? sg.heap : outc + ci;
                 t.blo = t.bhi = 0.f;
                 if constexpr (KT::BAND) {
                     const CutBounds cb = band_bounds(sg.pivot);
@@ -1142,8 +1313,8 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                 }
                 trav[s] = t;
             }
-            if (write) segs[s].child = (uint32_t)(outc + ci);
-            if (write) {
+            if (!leaves) {
+                segs[s].child = (uint32_t)(outc + ci);
                 uint64_t c = outc + ci;
                 const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
                 for (int side = 0; side < 2; ++side) {
@@ -1151,6 +1322,7 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                     if (!cn) continue;
                     Seg<KT> ch;
                     ch.off = side == 0 ? sg.off : sg.off + nl;
+                    ch.voff = outv + vi + (side == 0 ? 0 : nl);
                     ch.heap = side == 0 ? hl : hr;
                     ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
                     ch.prev = ~0ull;
@@ -1162,7 +1334,7 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                     ch.child = 0;
                     ch.xstate = 0;
                     ch.xkey = 0;
-                    ch.pad = 0;
+                    ch.set = sg.set;
                     ch.xcut = 0;
                     ch.xmin = ~0ull;
                     for (int d = 0; d < 3; ++d) {
@@ -1179,18 +1351,21 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                     ch.split_pos = 0;
                     next[c] = ch;
                     next_list[c] = (uint32_t)c;
-                    next_P[c] = ch.off;
+                    next_P[c] = ch.voff;
                     ++c;
                 }
             }
         }
         outc += tc;
+        outv += tv;
     }
     hmin = warp_min_u64(hmin);
-    if (!write && (threadIdx.x & 31) == 0) atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
+    if (!multi && (threadIdx.x & 31) == 0 && hmin != ~0ull)
+        atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
     if (threadIdx.x == 0) {
         rs->nsegs_next = outc;
-        if (write) next_P[outc] = n_total;
+        rs->items_next = outv;
+        if (write) next_P[outc] = outv;
     }
 }
 
@@ -1208,7 +1383,7 @@ template <int D, class KT, class WT>
 struct ReorderArgs {
     const Seg<KT> *segs;
     uint32_t S;
-    uint64_t n;
+    uint64_t n;  // items of the level's segments (chunks index their list, Seg::voff)
     uint64_t chunk;
     uint64_t nchunks;
     int coord;
@@ -1329,17 +1504,17 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         __syncthreads();
         const uint64_t t = s_ticket;
         if (t >= A.nchunks) break;
+        // [c0, c1): positions in the list of the level's items; a segment's
+        // items are at off + (position - voff)
         const uint64_t c0 = t * A.chunk, c1 = min(A.n, c0 + A.chunk);
-        const uint32_t kf = seg_index_of<KT>(A.segs, A.S, c0);
-        const uint32_t kl = seg_index_of<KT>(A.segs, A.S, c1 - 1);
-        auto piece_end = [&](uint32_t kk) {
-            const Seg<KT> &g = A.segs[kk];
-            return min(c1, g.off + g.n);
-        };
+        const uint32_t kf = seg_index_of_v<KT>(A.segs, A.S, c0);
+        const uint32_t kl = seg_index_of_v<KT>(A.segs, A.S, c1 - 1);
+        auto piece_end = [&](const Seg<KT> &g) { return g.off + (min(c1, g.voff + g.n) - g.voff); };
+        const Seg<KT> sf = A.segs[kf];
         TileRef cur;
         cur.kk = kf;
-        cur.ts = c0;
-        cur.pend = piece_end(kf);
+        cur.ts = sf.off + (c0 - sf.voff);
+        cur.pend = piece_end(sf);
         cur.te = min(cur.ts + R_TILE, cur.pend);
         cur.first = true;
         cur.valid = true;
@@ -1348,7 +1523,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         if (with_index) load_ix(cur, ixn);
         // count the left items of the last piece
         const Seg<KT> sl = A.segs[kl];
-        const uint64_t la = max(c0, sl.off);
+        const uint64_t la = sl.off + (max(c0, sl.voff) - sl.voff), le = sl.off + (c1 - sl.voff);
         uint64_t cnt = 0;
         {
             CutBounds spb = {0.f, 0.f};
@@ -1365,22 +1540,21 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             };
             // four loads in flight per thread
             uint64_t e = la + threadIdx.x;
-            for (; e + 3 * BLOCK < c1; e += 4 * BLOCK) {
+            for (; e + 3 * BLOCK < le; e += 4 * BLOCK) {
                 const K k0 = kc[e], k1 = kc[e + BLOCK], k2 = kc[e + 2 * BLOCK], k3 = kc[e + 3 * BLOCK];
                 cnt += left(k0, e) + left(k1, e + BLOCK) + left(k2, e + 2 * BLOCK) + left(k3, e + 3 * BLOCK);
             }
-            for (; e < c1; e += BLOCK) cnt += left(kc[e], e);
+            for (; e < le; e += BLOCK) cnt += left(kc[e], e);
         }
         uint64_t agg;
         block_exscan_u64(cnt, sh, agg);
-        const Seg<KT> sf = A.segs[kf];
         if (threadIdx.x == 0) {
-            const bool last_starts_here = sl.off >= c0;
+            const bool last_starts_here = sl.voff >= c0;
             s_fail = 0;
             if (last_starts_here) atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_INCL | agg));
             else atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_AGG | agg));
             uint64_t prefix = 0;
-            if (sf.off < c0) {
+            if (sf.voff < c0) {
                 // look back: chunk t-1 ends inside segment kf
                 int64_t j = (int64_t)t - 1;
                 for (;;) {
@@ -1438,7 +1612,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
                 nxt.kk = cur.kk + 1;
                 const Seg<KT> &g = A.segs[nxt.kk];
                 nxt.ts = g.off;
-                nxt.pend = min(c1, g.off + g.n);
+                nxt.pend = piece_end(g);
                 nxt.first = true;
                 nxt.valid = true;
             }
@@ -1709,6 +1883,83 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
                 left = left || KT::lt(kc, s_piv[e]);
             }
             if (i < n) part[i] = 2 * s_heap[seg[k]] + (left ? 1 : 2) - hmin;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_traverse_sets: k_traverse for several sets.  An item starts at its set's
+// root segment and walks its set's own number of levels; its id is relative
+// to the smallest heap id of its set.  Items of a set with iter_count 0 get
+// id 0.  Each CTA walks one contiguous range of items (few sets, so their
+// splits stay in L1), TRAV_ILP items per thread at once.
+// ---------------------------------------------------------------------------
+template <int D, class KT>
+__global__ void __launch_bounds__(BLOCK) k_traverse_sets(const Trav<KT> *__restrict__ trav, LevelOffsets lv,
+                                                         const typename KT::T *__restrict__ k0,
+                                                         const typename KT::T *__restrict__ k1,
+                                                         const typename KT::T *__restrict__ k2, uint64_t n,
+                                                         uint64_t *__restrict__ part, SetTab sets, BandSrc bs) {
+    typedef typename KT::T K;
+    constexpr uint64_t TILE = (uint64_t)BLOCK * TRAV_ILP;
+    const CtaRange r = cta_tiles((n + TILE - 1) / TILE, blockIdx.x, gridDim.x);
+    SetCursor cur;
+    for (uint64_t t = r.t0; t < r.t1; ++t) {
+        K key[TRAV_ILP][D];
+        uint64_t seg[TRAV_ILP], hmin[TRAV_ILP];
+        uint32_t depth[TRAV_ILP];
+        uint32_t maxd = 0;
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = t * TILE + (uint64_t)k * BLOCK + threadIdx.x;
+            depth[k] = 0;
+            seg[k] = 0;
+            hmin[k] = 0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) key[k][d] = K();
+            if (i < n) {
+                cur.move(sets, i);
+                const uint32_t root = sets.root[cur.s];
+                if (root != ~0u) {
+                    depth[k] = sets.iters[cur.s];
+                    seg[k] = root;
+                    hmin[k] = sets.minheap[cur.s];
+                }
+                key[k][0] = k0[i];
+                key[k][1] = k1[i];
+                if (D == 3) key[k][D - 1] = k2[i];
+                maxd = depth[k] > maxd ? depth[k] : maxd;
+            }
+        }
+        uint64_t id[TRAV_ILP] = {};
+        int c = 0;
+        for (uint32_t L = 0; L < maxd; ++L) {
+#pragma unroll
+            for (int k = 0; k < TRAV_ILP; ++k) {
+                if (L >= depth[k]) continue;
+                const uint64_t i = t * TILE + (uint64_t)k * BLOCK + threadIdx.x;
+                const Trav<KT> tr = trav[lv.off[L] + seg[k]];
+                const K kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
+                bool left = (tr.flags & TRAV_ALLLEFT) != 0;
+                if constexpr (KT::BAND) {
+                    if (!left) {
+                        const int sd = band_side(kc, CutBounds{tr.blo, tr.bhi});
+                        left = sd < 0 || (sd == 0 && KeyF64::lt(band_code(bs, i, c), tr.pivot));
+                    }
+                } else {
+                    left = left || KT::lt(kc, tr.pivot);
+                }
+                if (L + 1 < depth[k])
+                    seg[k] = tr.next + ((!left && (tr.flags & TRAV_HAS_LEFT)) ? 1 : 0);
+                else
+                    id[k] = 2 * tr.next + (left ? 1 : 2) - hmin[k];
+            }
+            c = c + 1 == D ? 0 : c + 1;
+        }
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = t * TILE + (uint64_t)k * BLOCK + threadIdx.x;
+            if (i < n) part[i] = id[k];
         }
     }
 }

@@ -62,9 +62,28 @@ struct Buffers {
     Trav<KT> *trav;  // finished splits of every level (traversal path only)
     RunScalars *rs;
     uint64_t hist_bins;
+    // several sets: the set table and the sets of the root segments
+    uint64_t *set_off, *set_bmin, *set_bmax, *set_wsum, *set_wabs, *set_minheap;
+    uint32_t *set_iters, *set_root, *roots;
+    int32_t *set_fs;
+
+    SetTab set_tab(uint32_t count) const {
+        SetTab t;
+        t.count = count;
+        t.off = set_off;
+        t.iters = set_iters;
+        t.root = set_root;
+        t.bmin = set_bmin;
+        t.bmax = set_bmax;
+        t.wsum = set_wsum;
+        t.wabs = set_wabs;
+        t.fs = set_fs;
+        t.minheap = set_minheap;
+        return t;
+    }
 
     size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap, bool index_path, bool carry,
-                 uint64_t tcap) {
+                 uint64_t tcap, uint64_t nsets = 0) {
         for (int k = 0; k < 3; ++k)
             for (int d = 0; d < 3; ++d) keys[k][d] = d < D ? b.take<K>(n) : nullptr;
         for (int s = 0; s < 2; ++s) {
@@ -82,6 +101,21 @@ struct Buffers {
         trav = index_path ? nullptr : b.take<Trav<KT>>(tcap);
         rs = b.take<RunScalars>(1);
         hist_bins = hb;
+        set_off = set_bmin = set_bmax = set_wsum = set_wabs = set_minheap = nullptr;
+        set_iters = set_root = roots = nullptr;
+        set_fs = nullptr;
+        if (nsets) {
+            set_off = b.take<uint64_t>(nsets + 1);
+            set_iters = b.take<uint32_t>(nsets);
+            set_root = b.take<uint32_t>(nsets);
+            roots = b.take<uint32_t>(nsets);
+            set_bmin = b.take<uint64_t>(nsets * 3);
+            set_bmax = b.take<uint64_t>(nsets * 3);
+            set_wsum = b.take<uint64_t>(nsets * 4);
+            set_wabs = b.take<uint64_t>(nsets);
+            set_fs = b.take<int32_t>(nsets);
+            set_minheap = b.take<uint64_t>(nsets);
+        }
         return b.off;
     }
 };
@@ -95,6 +129,9 @@ static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem
 // What the set-up of a run hands to its level loop.
 struct RunSetup {
     uint64_t n = 0, iters = 0, lbcap = 0, bytes = 0;
+    uint32_t nsets = 1;   // > 1: a batched run (set table in the buffers)
+    uint32_t nroots = 1;  // root segments on level 0
+    uint64_t v0 = 0;      // items of the root segments
     bool index_path = false;  // part ids from the segments (k_assign), not a traversal
     bool carry = false;       // reorders carry input indices (index path, band form)
     Mat M;                    // the basis change k_convert applied
@@ -126,21 +163,29 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     CG_CK(cudaFuncSetAttribute(reorder_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem));
     const int g_reorder = occupancy_grid(reorder_fn, C.sms, BLOCK, r_smem);
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
-    uint64_t chunk = std::max<uint64_t>(R_TILE, (n + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
-    chunk = (chunk + R_TILE - 1) / R_TILE * R_TILE;
-    const uint64_t nchunks = (n + chunk - 1) / chunk;
-    if (nchunks > R0.lbcap) {
-        *err = "internal: more reorder chunks than look-back words";
-        return COUPE_ERR_CRASH;
-    }
+    // reorder chunks over the V items of a level's segments
+    auto chunk_of = [&](uint64_t V) {
+        uint64_t c = std::max<uint64_t>(R_TILE, (V + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
+        return (c + R_TILE - 1) / R_TILE * R_TILE;
+    };
+    const bool multi = R0.nsets > 1;
+    const SetTab sets = B.set_tab(R0.nsets);
+    const int32_t *set_fs = multi && WL::LIMBS > 1 ? B.set_fs : nullptr;
     const int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
-    CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
+    if (multi) {
+        CG_LAUNCH(KID_ROOT, 0,
+                  k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,
+                                                                           R0.nroots, D, sets));
+    } else {
+        CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
+    }
     const uint64_t sk = sizeof(K), sw = sizeof(WS), si = carry ? 4 : 0;
 
     int kb = 0;          // key buffer of the current level
     int sb = 0;          // segment table / weight buffer of the current level
     bool level0 = true;  // level 0 reads the caller's weights and implicit indices
-    uint64_t S = 1;
+    uint64_t S = R0.nroots;
+    uint64_t V = R0.v0;  // items of the level's segments
     LevelOffsets lv;
     uint64_t trav_used = 0;
     // bins per segment: as many bisection steps per pass as the budget allows
@@ -149,7 +194,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         while (k > 1 && nseg * (1ull << k) > B.hist_bins) --k;
         return k;
     };
-    int nbk = pick_nbk(1);
+    int nbk = pick_nbk(S);
     int err_level = -1;  // level at whose synchronisation a device check was first seen
     Hist<KT, WL> H{B.hcnt, B.hw, B.hinv};
     for (uint64_t L = 0; L < iters; ++L) {
@@ -171,8 +216,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         const uint32_t *hsrc = KT::BAND ? ic : nullptr;
         auto children = [&]() {
             CG_LAUNCH(KID_CHILDREN, 0,
-                      k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, B.segs[snext],
-                                                            B.list[0], B.P[0], n, trav_l, B.rs));
+                      k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, (uint32_t)L,
+                                                            B.segs[snext], B.list[0], B.P[0], trav_l, B.rs, sets));
             return (int)COUPE_ERR_OK;
         };
         const unsigned decide_grid = (unsigned)((S + NWARPS - 1) / NWARPS);
@@ -182,15 +227,15 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
         CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WL::LIMBS * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
-        CG_LAUNCH(KID_HIST, n * (sk + sw),
+        CG_LAUNCH(KID_HIST, V * (sk + sw),
                   k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], (uint32_t)S, kc, wc, H, nbk, n,
-                                                          B.rs, 0, hsrc, bs, coord, segs));
+                                                          B.rs, 0, hsrc, bs, coord, segs, set_fs));
         ++st->hist_passes;
-        st->hist_points += n;
-        bytes += n * (sk + sw);
+        st->hist_points += V;
+        bytes += V * (sk + sw);
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
-                                                                 B.flags, B.rs, 0));
+                                                                 B.flags, B.rs, 0, set_fs));
         CG_LAUNCH(KID_SCAN, 0,
                   k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[0], B.flags, (uint32_t)S, B.list[1], B.P[1], B.rs, 0));
         // A speculative second pass over list[1] without asking the host how
@@ -198,11 +243,11 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         // once when no segment is searching.  The next scan leaves list[0].
         CG_LAUNCH(KID_HIST, 0,
                   k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1, hsrc,
-                                                          bs, coord, segs));
+                                                          bs, coord, segs, set_fs));
         ++st->hist_passes;
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
-                                                                 B.rs, 1));
+                                                                 B.rs, 1, set_fs));
         CG_LAUNCH(KID_SCAN, 0,
                   k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[1], B.flags, 0, B.list[0], B.P[0], B.rs, 1));
         // k_children returns at once if a segment is still searching
@@ -229,11 +274,11 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             const uint64_t nlist = h_rs->nactive;
             CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
                       k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs));
+                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs, set_fs));
             ++st->hist_passes;
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
-                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0));
+                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs));
             CG_LAUNCH(KID_SCAN, 0,
                       k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
                                                          B.P[li ^ 1], B.rs, 0));
@@ -259,7 +304,12 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             }
         }
         if (last) {
-            if (index_path) {
+            if (multi) {
+                CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                          k_traverse_sets<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, lv, B.keys[0][0], B.keys[0][1],
+                                                                            B.keys[0][2], n, a.d_part, sets, bs));
+                bytes += n * (D * sk + 8);
+            } else if (index_path) {
                 CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
                           k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs, bs,
                                                                   coord));
@@ -283,14 +333,20 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             st->levels = L + 1;
             break;
         }
-        const uint64_t S_next = h_rs->nsegs_next;
+        const uint64_t S_next = h_rs->nsegs_next, V_next = h_rs->items_next;
+        const uint64_t chunk = chunk_of(V);
+        const uint64_t nchunks = (V + chunk - 1) / chunk;
+        if (nchunks > R0.lbcap) {
+            *err = "internal: more reorder chunks than look-back words";
+            return COUPE_ERR_CRASH;
+        }
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
         const int kb_next = kb == 1 ? 2 : 1;
         ReorderArgs<D, KT, WL> R;
         R.segs = segs;
         R.S = (uint32_t)S;
-        R.n = n;
+        R.n = V;
         R.chunk = chunk;
         R.nchunks = nchunks;
         R.coord = coord;
@@ -305,18 +361,19 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         R.bs = bs;
         R.lb = B.lb;
         R.rs = B.rs;
-        const uint64_t rbytes = 2 * n * (D * sk + sw + si) - (ic ? 0 : n * si);
+        const uint64_t rbytes = 2 * V * (D * sk + sw + si) - (ic ? 0 : V * si);
         const unsigned r_grid = (unsigned)std::min<uint64_t>(g_reorder, nchunks);
         if (carry) {
             CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, true><<<r_grid, BLOCK, r_smem, s>>>(R));
         } else {
             CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, false><<<r_grid, BLOCK, r_smem, s>>>(R));
         }
-        bytes += n * sk /* flag pre-count */ + rbytes;
+        bytes += V * sk /* flag pre-count */ + rbytes;
         kb = kb_next;
         sb = snext;
         level0 = false;
         S = S_next;
+        V = V_next;
         nbk = pick_nbk(S_next);
         st->levels = L + 1;
     }
@@ -367,7 +424,28 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         *err = "more than 2^32 - 1 points";
         return COUPE_ERR_ALLOC;
     }
-    if (a.iter_count == 0) {
+    const bool multi = a.nsets > 1;
+    // Several sets: root segments for the non-empty sets with iter_count > 0,
+    // in set order; the deepest set gives the number of levels.
+    std::vector<uint32_t> h_root, h_roots;
+    std::vector<uint64_t> h_P;
+    uint64_t v0 = n, max_iters = a.iter_count;
+    if (multi) {
+        h_root.assign(a.nsets, ~0u);
+        v0 = 0;
+        max_iters = 0;
+        for (uint64_t k = 0; k < a.nsets; ++k) {
+            const uint64_t nk = a.set_off[k + 1] - a.set_off[k];
+            if (nk == 0 || a.set_iters[k] == 0) continue;
+            h_root[k] = (uint32_t)h_roots.size();
+            h_roots.push_back((uint32_t)k);
+            h_P.push_back(v0);
+            v0 += nk;
+            max_iters = std::max<uint64_t>(max_iters, a.set_iters[k]);
+        }
+        h_P.push_back(v0);
+    }
+    if (max_iters == 0) {
         // rcb_recurse with iter_count == 0 stores id 0 everywhere (:589-602)
         CG_LAUNCH(KID_FILL, n * 8,
                   k_fill_u64<<<std::max<uint64_t>(1, std::min<uint64_t>((n + 255) / 256, 4096)), 256, 0, s>>>(a.d_part,
@@ -375,16 +453,38 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         CG_CK(cudaStreamSynchronize(s));
         return COUPE_ERR_OK;
     }
-    const uint64_t iters = a.iter_count;
-    // segment capacity: a level holds at most min(2^level, n) segments
-    uint64_t scap = iters >= 40 ? n : std::min<uint64_t>(n, 1ull << iters);
-    scap = std::max<uint64_t>(scap, 1);
+    const uint64_t iters = max_iters;
+    uint64_t scap = 1, tcap = 0;
+    bool index_path = false;
+    if (multi) {
+        // level L holds at most min(2^L, n_k) segments of each set deeper than L
+        for (uint64_t L = 0; L < iters && L < 64; ++L) {
+            uint64_t cnt = 0;
+            for (uint32_t k : h_roots) {
+                const uint64_t nk = a.set_off[k + 1] - a.set_off[k];
+                if (a.set_iters[k] > L) cnt += L < 40 ? std::min<uint64_t>(nk, 1ull << L) : nk;
+            }
+            scap = std::max(scap, cnt);
+            tcap += cnt;
+        }
+        scap = std::max<uint64_t>(scap, h_roots.size());
+        if (iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES) {
+            *err = "batched run: more than " + std::to_string(MAX_TRAV_LEVELS) + " levels or " +
+                   std::to_string(TRAV_MAX_ENTRIES) + " splits";
+            return COUPE_ERR_ALLOC;
+        }
+    } else {
+        // segment capacity: a level holds at most min(2^level, n) segments
+        scap = iters >= 40 ? n : std::min<uint64_t>(n, 1ull << iters);
+        scap = std::max<uint64_t>(scap, 1);
+        // Part ids come from a traversal of the recorded splits unless the
+        // tree is too large to record; then every reorder carries the input
+        // indices.
+        for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L)
+            tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
+        index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
+    }
     const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
-    // Part ids come from a traversal of the recorded splits unless the tree is
-    // too large to record; then every reorder carries the input indices.
-    uint64_t tcap = 0;
-    for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L) tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
-    const bool index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
     // look-back words: one per reorder chunk; a reorder grid never exceeds 8
     // CTAs of BLOCK threads per SM, so this capacity fits every weight type
     const uint64_t lbcap = (uint64_t)C.sms * 8 * (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
@@ -392,11 +492,13 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     Buffers<D, KT, WT> B;
     Bump dry{nullptr, 0};
     const bool carry = index_path || KT::BAND;
-    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap);
+    const uint64_t nsets = multi ? a.nsets : 0;
+    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
     int rc = ensure_workspace(C, need, err);
     if (rc != COUPE_ERR_OK) return rc;
     Bump real{(char *)C.ws, 0};
-    B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap);
+    B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
+    const SetTab sets = B.set_tab(multi ? (uint32_t)a.nsets : 1u);
     RunScalars *h_rs = (RunScalars *)C.h_pinned;
 
     const int g_stream = std::max<int>(1, std::min<uint64_t>((n + BLOCK - 1) / BLOCK, (uint64_t)C.sms * 8));
@@ -411,6 +513,17 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     init.min_heap = ~0ull;
     *h_rs = init;
     CG_CK(cudaMemcpyAsync(B.rs, h_rs, sizeof(RunScalars), cudaMemcpyHostToDevice, s));
+    if (multi) {
+        // the set table (pageable copies: the host vectors are read before
+        // the calls return)
+        const uint64_t nr = h_roots.size();
+        CG_CK(cudaMemcpyAsync(B.set_off, a.set_off, (nsets + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        CG_CK(cudaMemcpyAsync(B.set_iters, a.set_iters, nsets * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CG_CK(cudaMemcpyAsync(B.set_root, h_root.data(), nsets * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CG_CK(cudaMemcpyAsync(B.roots, h_roots.data(), nr * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        CG_CK(cudaMemcpyAsync(B.P[0], h_P.data(), (nr + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        CG_LAUNCH(KID_ROOT, 0, k_sets_init<<<(unsigned)((nsets + 255) / 256), 256, 0, s>>>(sets));
+    }
 
     Mat M;
     std::memset(&M, 0, sizeof(M));
@@ -419,20 +532,24 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
     CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
               k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
-                                                          B.rs));
+                                                          B.rs, sets));
     const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
     if (WT::LIMBS > 1) {
-        CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs));
+        CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs, sets));
+        if (multi) CG_LAUNCH(KID_WABS, 0, k_set_fs<<<(unsigned)((nsets + 255) / 256), 256, 0, s>>>(sets, B.rs));
     }
     // integer weights: the weight sum also writes a 16-bit copy into w[0]
     // (which level 0 does not otherwise use) for the level loop to read when
     // every weight lies in [0, 2^16)
     uint16_t *c16 = WT::LIMBS == 1 ? (uint16_t *)B.w[0] : nullptr;
-    CG_LAUNCH(KID_WSUM, n * sw + (c16 ? n * 2 : 0), k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs, c16));
+    CG_LAUNCH(KID_WSUM, n * sw + (c16 ? n * 2 : 0), k_wsum<WT><<<g_stream, BLOCK, 0, s>>>(w_in, n, B.rs, c16, sets));
 
     RunSetup R0;
     R0.n = n;
-    R0.iters = a.iter_count;
+    R0.iters = iters;
+    R0.nsets = multi ? (uint32_t)a.nsets : 1u;
+    R0.nroots = multi ? (uint32_t)h_roots.size() : 1u;
+    R0.v0 = v0;
     R0.index_path = index_path;
     R0.carry = carry;
     R0.M = M;

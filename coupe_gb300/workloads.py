@@ -42,22 +42,45 @@ def planes3d_lognormal(n=67_108_864, seed=0):
     return pts, w, dict(iter_count=12, tolerance=0.005, name="planes3d_67M_4096parts")
 
 
-def batched_sets(n_sets=4096, seed=0, total=200_000_000):
-    """4: n_sets independent point sets, sizes lognormal clipped to
-    [1e3, 1e6] scaled to about `total` points, half 2D half 3D, coordinates
-    uniform in a per-set random box, int64 weights U{1..10}, iter_count
-    U{1..8} per set.  Returns a list of (points, weights, iter_count)."""
+def _batched_iter(n_sets, seed, total):
     rng = np.random.default_rng(seed)
     raw = rng.lognormal(0.0, 1.0, size=n_sets)
     sizes = np.clip(raw / raw.sum() * total, 1_000, 1_000_000).astype(np.int64)
-    out = []
     for s in range(n_sets):
         d = 2 if s % 2 == 0 else 3
         lo = rng.random(d) * 100.0
         span = 1.0 + rng.random(d) * 99.0
         pts = lo + rng.random((int(sizes[s]), d)) * span
         w = rng.integers(1, 11, size=int(sizes[s]), dtype=np.int64)
-        out.append((pts, w, int(rng.integers(1, 9))))
+        yield s, pts, w, int(rng.integers(1, 9))
+
+
+def batched_sets(n_sets=4096, seed=0, total=200_000_000):
+    """4: n_sets independent point sets, sizes lognormal clipped to
+    [1e3, 1e6] scaled to about `total` points, half 2D half 3D, coordinates
+    uniform in a per-set random box, int64 weights U{1..10}, iter_count
+    U{1..8} per set.  Returns a list of (points, weights, iter_count)."""
+    return [(p, w, it) for _, p, w, it in _batched_iter(n_sets, seed, total)]
+
+
+def batched_groups(n_sets=4096, seed=0, total=200_000_000):
+    """The sets of batched_sets (same values), concatenated per dimension in
+    set order, as one batched call per dimension takes them:
+    {dim: (points (N, dim), weights (N,), set offsets (k + 1,), iter counts
+    (k,), set numbers (k,))}."""
+    parts = {2: [], 3: []}
+    for s, p, w, it in _batched_iter(n_sets, seed, total):
+        parts[p.shape[1]].append((s, p, w, it))
+    out = {}
+    for d, lst in parts.items():
+        if not lst:
+            continue
+        sizes = np.array([len(p) for _, p, _, _ in lst], dtype=np.uint64)
+        off = np.zeros(len(lst) + 1, dtype=np.uint64)
+        np.cumsum(sizes, out=off[1:])
+        out[d] = (np.concatenate([p for _, p, _, _ in lst]), np.concatenate([w for _, _, w, _ in lst]), off,
+                  np.array([it for _, _, _, it in lst], dtype=np.uint32),
+                  np.array([s for s, _, _, _ in lst], dtype=np.int64))
     return out
 
 

@@ -70,6 +70,22 @@ enum coupe_err coupe_gpu_rcb_device(uint64_t *d_partition, uint64_t n, uint64_t 
 		uint64_t iter_count, double tolerance, int mode, const double *matrix,
 		void *stream);
 
+/* Batched Rcb on device-resident inputs: `nsets` independent point sets of
+ * one dimension partitioned in one run (no counterpart in the reference; the
+ * same result as one coupe_gpu_rcb_device call per set).  Set k is points
+ * [set_offsets[k], set_offsets[k + 1]) of `d_points` / `d_weights` /
+ * `d_partition` and is split into at most 2^iter_counts[k] parts; its ids
+ * start at 0 like a run of that set alone.  `set_offsets` (nsets + 1
+ * entries, starting at 0, non-decreasing) and `iter_counts` (nsets entries)
+ * are host arrays.  Empty sets are allowed; a set with iter_count 0 gets id
+ * 0 everywhere.  Limits: 2^32 - 1 points in all, at most 63 levels, and at
+ * most 2^22 splits over all sets (else COUPE_ERR_ALLOC).  Returns after the
+ * work on `stream` completed. */
+enum coupe_err coupe_gpu_rcb_batched(uint64_t *d_partition, uint64_t nsets,
+		const uint64_t *set_offsets, uint64_t dimension, const double *d_points,
+		enum coupe_type weight_type, const void *d_weights,
+		const uint32_t *iter_counts, double tolerance, int mode, void *stream);
+
 /* Rib on device-resident inputs (see coupe_gpu_rcb_device). */
 enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
 		const double *d_points, enum coupe_type weight_type, const void *d_weights,

@@ -92,6 +92,18 @@ def rcb(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, thr
     return out, st.as_dict()
 
 
+def rcb_sets(points, weights, set_offsets, iter_counts, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1):
+    """Part ids of independent Rcb runs, one per set (rows set_offsets[k]:
+    set_offsets[k + 1], iter_counts[k]); each set's ids start at 0."""
+    p, w = _prep(points, weights)
+    out = np.zeros(len(p), dtype=np.uint64)
+    for k, it in enumerate(iter_counts):
+        a, b = int(set_offsets[k]), int(set_offsets[k + 1])
+        if b > a:
+            out[a:b], _ = rcb(p[a:b], w[a:b], int(it), tolerance, mode=mode, fsum=fsum, threads=threads)
+    return out
+
+
 def rib(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1, matrix=None):
     p, w = _prep(points, weights)
     n, dim = p.shape

@@ -86,3 +86,25 @@ def test_data_free_null_is_noop(coupe):
 
 def test_version(coupe):
     assert b"sm_103a" in coupe.lib().coupe_gpu_version()
+
+
+def test_batched_arguments_checked_before_the_device(coupe):
+    """coupe_gpu_rcb_batched validates its host arrays before any device
+    work: the device pointers below are never dereferenced."""
+    L = coupe.lib()
+    f = L.coupe_gpu_rcb_batched
+    it = np.array([3, 3], dtype=np.uint32)
+    bad_start = np.array([1, 5, 9], dtype=np.uint64)
+    decreasing = np.array([0, 5, 4], dtype=np.uint64)
+    empty = np.array([0, 0, 0], dtype=np.uint64)
+    dev = 256  # placeholder device addresses, never used
+    assert f(dev, 2, bad_start.ctypes.data, 2, dev, coupe.COUPE_INT64, dev, it.ctypes.data, 0.1, 0, None) == \
+        coupe.ERR_LEN_MISMATCH
+    assert f(dev, 2, decreasing.ctypes.data, 2, dev, coupe.COUPE_INT64, dev, it.ctypes.data, 0.1, 0, None) == \
+        coupe.ERR_LEN_MISMATCH
+    assert f(dev, 2, empty.ctypes.data, 4, dev, coupe.COUPE_INT64, dev, it.ctypes.data, 0.1, 0, None) == \
+        coupe.ERR_BAD_DIMENSION
+    assert f(dev, 2, empty.ctypes.data, 3, dev, 7, dev, it.ctypes.data, 0.1, 0, None) == coupe.ERR_BAD_TYPE
+    assert f(dev, 0, None, 3, dev, coupe.COUPE_INT64, dev, None, 0.1, 0, None) == coupe.ERR_OK
+    assert f(dev, 2, empty.ctypes.data, 3, dev, coupe.COUPE_INT64, dev, it.ctypes.data, 0.1, 0, None) == coupe.ERR_OK
+    assert f(dev, 2, None, 3, dev, coupe.COUPE_INT64, dev, None, 0.1, 0, None) == coupe.ERR_LEN_MISMATCH
