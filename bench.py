@@ -6,6 +6,7 @@ Inputs are 537 MB per step (larger than the 129 MB L2), so no L2 flush is
 needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload gauss16M|planes67M|batched4096|hexrib134M]
 
 `value`   device-resident throughput (inputs in HBM before the timed region),
           Mpoints/s, of the headline precision mode.
@@ -17,6 +18,10 @@ needed between steps.
 `cpu_baseline` the CPU restatement of coupe's Rcb (OpenMP, all host cores).
 --impl reference times that CPU restatement alone (the reference itself is
 Rust and cannot be built here).
+
+The other workloads (--workload) print one line of the same form for the
+precision form on 67M points (4096 parts, f64 weights), the batched form
+(4096 sets, ~2e8 points) and Rib on a 512^3 hex mesh (134M points).
 """
 import argparse
 import json
@@ -44,6 +49,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--points", type=int, default=16_777_216)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--workload", default="gauss16M", choices=["gauss16M", "planes67M", "batched4096", "hexrib134M"])
     return ap.parse_args()
 
 
@@ -182,6 +188,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.workload != "gauss16M":
+        return run_workload(args)
     if args.impl == "reference":
         return run_reference(args)
     import torch
@@ -324,6 +332,168 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+    return 0
+
+
+def run_workload(args):
+    """One line for a non-headline workload: every precision mode timed on
+    device-resident inputs, the band form end to end from pinned host
+    buffers, the top kernel's roofline and the oracle on the host cores."""
+    import torch
+    import coupe_gb300 as coupe
+    from coupe_gb300 import workloads
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    coupe.lib()
+    t_gen = time.perf_counter()
+    if args.workload == "batched4096":
+        groups = workloads.batched_groups()
+        tol = 0.01
+        sets = {d: (torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev), off, it)
+                for d, (p, w, off, it, _) in groups.items()}
+        hosts = {d: (p, w) for d, (p, w, _, _, _) in groups.items()}
+        n = sum(len(p) for p, _ in hosts.values())
+        outs = {d: torch.empty(len(hosts[d][0]), dtype=torch.int64, device=dev) for d in sets}
+        cfg = {"workload": "batched_4096sets", "sets": 4096, "points": n, "dim": "2 and 3 (one call each)",
+               "iter_count": "U{1..8} per set", "tolerance": tol, "weights": "int64 U{1..10}"}
+
+        def step(mode):
+            for d, (p, w, off, it) in sets.items():
+                coupe.rcb_batched_device(outs[d], p, w, off, it, tol, mode=mode)
+
+        def ids():
+            return {d: o.cpu().numpy().view(np.uint64).copy() for d, o in outs.items()}
+
+        def cpu_run():
+            return {d: oracle.rcb_sets(p, w, off, it, tol, threads=0) for d, (p, w, off, it, _) in groups.items()}
+    else:
+        rib = args.workload == "hexrib134M"
+        pts_h, w_h, c = workloads.hex_mesh_rib() if rib else workloads.planes3d_lognormal()
+        iters, tol = c["iter_count"], c["tolerance"]
+        n = len(pts_h)
+        hosts = {3: (pts_h, w_h)}
+        p_d, w_d = torch.from_numpy(pts_h).to(dev), torch.from_numpy(w_h).to(dev)
+        out = torch.empty(n, dtype=torch.int64, device=dev)
+        outs = {3: out}
+        cfg = {"workload": c["name"], "points": n, "dim": 3, "parts": 1 << iters, "iter_count": iters,
+               "tolerance": tol, "weights": "float64", "algorithm": "Rib" if rib else "Rcb"}
+
+        def step(mode):
+            (coupe.rib_device if rib else coupe.rcb_device)(out, p_d, w_d, iters, tol, mode=mode)
+
+        def ids():
+            return {3: out.cpu().numpy().view(np.uint64).copy()}
+
+        def cpu_run():
+            return {3: (oracle.rib if rib else oracle.rcb)(pts_h, w_h, iters, tol, threads=0)[0]}
+    t_gen = time.perf_counter() - t_gen
+    stream = torch.cuda.current_stream()
+    modes = ["ref32", "f64", "f32key_f64band"]
+    results, launches, got, mstats = {}, {}, {}, {}
+    clocks = None
+    for mode in modes:
+        for _ in range(args.warmup):
+            step(mode)
+        torch.cuda.synchronize()
+        st = coupe.last_stats()
+        mstats[mode] = {k: st[k] for k in ("hist_passes", "hist_points", "band_points", "kernel_launches", "splits",
+                                           "split_steps", "max_split_steps", "algo_bytes")}
+        if mode == "f32key_f64band":
+            clocks = Clocks(0).__enter__()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nl = 0
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step(mode)
+            nl += coupe.last_stats()["kernel_launches"]
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        if mode == "f32key_f64band":
+            clocks.__exit__()
+        results[mode] = ev0.elapsed_time(ev1) / args.steps
+        launches[mode] = nl
+        got[mode] = ids()
+    by_mode = {}
+    for mode in modes:
+        coupe.profile(True)
+        for _ in range(args.steps):
+            step(mode)
+        torch.cuda.synchronize()
+        by_mode[mode] = coupe.profile_read()
+        coupe.profile(False)
+    prof = by_mode["f32key_f64band"]
+    total_ms = sum(v["ms"] for v in prof.values()) or 1.0
+    top = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    peak, peak_kind = measured_peak()
+    achieved = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": top[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
+                "share": round(top[1]["ms"] / total_ms, 3),
+                "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                "share": round(v["ms"] / total_ms, 3)}
+                            for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}
+    # end to end: pinned host inputs copied in, ids copied out, every step
+    pins = {d: (torch.from_numpy(p).pin_memory(), torch.from_numpy(w).pin_memory(),
+                torch.empty(len(p), dtype=torch.int64).pin_memory()) for d, (p, w) in hosts.items()}
+    dsts = {d: (torch.empty(tuple(p.shape), dtype=p.dtype, device=dev), torch.empty(len(w), dtype=w.dtype, device=dev))
+            for d, (p, w, _) in pins.items()}
+
+    def e2e_step():
+        for d, (hp, hw, ho) in pins.items():
+            dsts[d][0].copy_(hp, non_blocking=True)
+            dsts[d][1].copy_(hw, non_blocking=True)
+        if args.workload == "batched4096":
+            for d, (_, _, off, it) in sets.items():
+                coupe.rcb_batched_device(outs[d], dsts[d][0], dsts[d][1], off, it, tol, mode="f32key_f64band")
+        else:
+            (coupe.rib_device if args.workload == "hexrib134M" else coupe.rcb_device)(
+                outs[3], dsts[3][0], dsts[3][1], cfg["iter_count"], tol, mode="f32key_f64band")
+        for d, (_, _, ho) in pins.items():
+            ho.copy_(outs[d], non_blocking=True)
+        torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        e2e_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    t_e2e = (time.perf_counter() - t0) / args.steps
+    e2e_ok = all(np.array_equal(pins[d][2].numpy().view(np.uint64), got["f32key_f64band"][d]) for d in pins)
+    parity = {"band_vs_f64_mismatches": int(sum((got["f32key_f64band"][d] != got["f64"][d]).sum() for d in got["f64"])),
+              "e2e_ids_equal_device_ids": e2e_ok}
+    cpu = None
+    if not args.no_cpu:
+        t0 = time.perf_counter()
+        ref = cpu_run()
+        t_cpu = time.perf_counter() - t0
+        parity["ref32_vs_oracle_mismatches"] = int(sum((ref[d] != got["ref32"][d]).sum() for d in ref))
+        cpu = {"value": round(n / t_cpu / 1e6, 2), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+               "sample": "full workload, one run (%.2f s); OpenMP restatement of coupe %s" %
+                         (t_cpu, cfg.get("algorithm", "Rcb"))}
+    ms = results["f32key_f64band"]
+    h2d = sum(p.nbytes + w.nbytes for p, w in hosts.values())
+    line = {
+        "metric": "%s Mpoints/s, %s: FP32-key+FP64-band vs plain FP64 on GB300" % (
+            cfg.get("algorithm", "RCB").upper(), cfg["workload"]),
+        "value": round(n / (ms / 1e3) / 1e6, 2), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": cfg,
+        "modes": {m: {"ms_per_step": round(results[m], 4), "value": round(n / (results[m] / 1e3) / 1e6, 2)}
+                  for m in results},
+        "band_vs_f64_speedup": round(results["f64"] / results["f32key_f64band"], 3),
+        "e2e": {"value": round(n / t_e2e / 1e6, 2), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(n * 8), "ms_per_step": round(t_e2e * 1e3, 3)},
+        "gpu_launches": launches["f32key_f64band"], "roofline": roofline, "parity": parity,
+        "run": {"last_call_stats": mstats,
+                "kernel_ms_per_step": {m: {k: round(v["ms"] / args.steps, 3) for k, v in pr.items()}
+                                       for m, pr in by_mode.items()}},
+        "clocks": clocks.summary() if clocks else None, "generation_s": round(t_gen, 1),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
     return 0
 
 

@@ -203,7 +203,7 @@ struct BandSrc {
     double m[3][3];
     int on;
     int D;
-    unsigned long long *count;  // coordinates read (the run's band_points)
+    unsigned long long *count;  // coordinates read by histogram passes (the run's band_points)
 };
 inline BandSrc make_band_src(const double *pts, const Mat &M, int D, unsigned long long *count) {
     BandSrc b;
@@ -233,7 +233,6 @@ __device__ __forceinline__ uint64_t band_code(const BandSrc &bs, uint64_t orig, 
     } else {
         x = p[coord];
     }
-    atomicAdd(bs.count, 1ull);
     return KeyF64::from_f64(x);
 }
 // The same, out of line: for the rare band items of hot loops, so that the
@@ -759,6 +758,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         bool xpend = false;  // band form: a decision waits for an exact minimum
         uint32_t xkey = 0;
         uint64_t xcut = 0;
+        uint64_t xm = ~0ull;  // band form: this thread's part of that minimum
+        uint32_t nband = 0;   // band form: f64 coordinates this thread read
         if constexpr (KT::BAND) {
             blo = band_bounds(lo);
             bhi = band_bounds(hi);
@@ -843,8 +844,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                     const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
                     const K kk = keys[e];
                     const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
-                    if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut))
-                        atomicMin((unsigned long long *)&segs_w[s].xmin, (unsigned long long)c);
+                    ++nband;
+                    if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
                     uint64_t q[L];
                     WT::limbs(wts[e], fs, q);
                     const O v = (O)~KT::ord(kk);
@@ -913,6 +914,16 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                     if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
                 }
             }
+            }
+        }
+        if constexpr (KT::BAND) {
+            // one global update per warp and piece: a plane of equal
+            // coordinates can put millions of items in one band
+            const uint64_t xw = warp_min_u64(xm);
+            const uint64_t nw = warp_sum_u64(nband);
+            if ((threadIdx.x & 31) == 0) {
+                if (xw != ~0ull) atomicMin((unsigned long long *)&segs_w[s].xmin, (unsigned long long)xw);
+                if (nw) atomicAdd(bs.count, (unsigned long long)nw);
             }
         }
         // fold the out-of-interval sums into the edge bins (one lane per warp)
@@ -1258,10 +1269,14 @@ __global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ 
 // (2h+2, sum - weight_left, bbox min[coord] = split_pos), empty children
 // dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
 // the smallest heap id among the children (the id offset, :698-702).
+enum : int { CHILD_ALL = 0, CHILD_COUNT = 1, CHILD_SCAN = 2, CHILD_WRITE = 3 };
+constexpr uint32_t CHILD_GRID_MIN = 2048;  // segments from which a level uses the grid form
+
 template <class KT, class WT>
 __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
                                                    uint32_t level, Seg<KT> *next, uint32_t *next_list,
-                                                   uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets) {
+                                                   uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets,
+                                                   int phase, uint64_t *blk) {
     typedef typename KT::T K;
     __shared__ uint64_t sh[33];
     // launched right after a speculative pass: nothing to do while a segment
@@ -1271,7 +1286,42 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
     uint64_t outc = 0, outv = 0;
     uint64_t hmin = ~0ull;
     const int nc = (coord + 1) % D;
-    for (uint32_t base = 0; base < S; base += blockDim.x) {
+    // CHILD_ALL: one CTA walks every segment.  Levels with many segments use
+    // a grid of CTAs, one per 1024 segments, in three launches:
+    // CHILD_COUNT (each CTA's children and items into blk), CHILD_SCAN (one
+    // CTA: blk becomes exclusive offsets) and CHILD_WRITE.
+    uint32_t first = 0, stop = S;
+    if (phase == CHILD_COUNT || phase == CHILD_WRITE) {
+        first = blockIdx.x * blockDim.x;
+        stop = min(S, first + blockDim.x);
+        if (phase == CHILD_WRITE) {
+            outc = blk[2 * blockIdx.x];
+            outv = blk[2 * blockIdx.x + 1];
+        }
+    }
+    if (phase == CHILD_SCAN) {
+        const uint32_t nb = (S + 1023) / 1024;
+        for (uint32_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+            const uint32_t b = b0 + threadIdx.x;
+            const uint64_t c = b < nb ? blk[2 * b] : 0, v = b < nb ? blk[2 * b + 1] : 0;
+            uint64_t tc, tv;
+            const uint64_t ci = block_exscan_u64(c, sh, tc);
+            const uint64_t vi = block_exscan_u64(v, sh, tv);
+            if (b < nb) {
+                blk[2 * b] = outc + ci;
+                blk[2 * b + 1] = outv + vi;
+            }
+            outc += tc;
+            outv += tv;
+        }
+        if (threadIdx.x == 0) {
+            rs->nsegs_next = outc;
+            rs->items_next = outv;
+            if (write) next_P[outc] = outv;
+        }
+        return;
+    }
+    for (uint32_t base = first; base < stop; base += blockDim.x) {
         const uint32_t s = base + threadIdx.x;
         Seg<KT> sg;
         uint32_t nl = 0, nr = 0;
@@ -1289,7 +1339,14 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
         uint64_t tc, tv;
         const uint64_t ci = block_exscan_u64(leaves ? 0 : (nl > 0) + (nr > 0), sh, tc);
         const uint64_t vi = block_exscan_u64(leaves ? 0 : (uint64_t)nl + nr, sh, tv);
-        if (s < S) {
+        if (phase == CHILD_COUNT) {
+            if (threadIdx.x == 0) {
+                blk[2 * blockIdx.x] = tc;
+                blk[2 * blockIdx.x + 1] = tv;
+            }
+            return;
+        }
+        if (s < stop) {
             const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
             if (leaves) {
                 uint64_t h = ~0ull;
@@ -1362,7 +1419,7 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
     hmin = warp_min_u64(hmin);
     if (!multi && (threadIdx.x & 31) == 0 && hmin != ~0ull)
         atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
-    if (threadIdx.x == 0) {
+    if (phase == CHILD_ALL && threadIdx.x == 0) {
         rs->nsegs_next = outc;
         rs->items_next = outv;
         if (write) next_P[outc] = outv;

@@ -59,6 +59,7 @@ struct Buffers {
     uint64_t *hw;
     O *hinv;
     uint64_t *lb;
+    uint64_t *blk;   // per-CTA child counts of the grid form of k_children
     Trav<KT> *trav;  // finished splits of every level (traversal path only)
     RunScalars *rs;
     uint64_t hist_bins;
@@ -98,6 +99,7 @@ struct Buffers {
         hw = b.take<uint64_t>(hb * WT::LIMBS);
         hinv = b.take<O>(hb);
         lb = b.take<uint64_t>(lbcap);
+        blk = b.take<uint64_t>(2 * (scap / 1024 + 1));
         trav = index_path ? nullptr : b.take<Trav<KT>>(tcap);
         rs = b.take<RunScalars>(1);
         hist_bins = hb;
@@ -215,9 +217,21 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         // band form: the items' input indices, for coordinates in the band
         const uint32_t *hsrc = KT::BAND ? ic : nullptr;
         auto children = [&]() {
-            CG_LAUNCH(KID_CHILDREN, 0,
-                      k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, last ? 0 : 1, (uint32_t)L,
-                                                            B.segs[snext], B.list[0], B.P[0], trav_l, B.rs, sets));
+            const int wr = last ? 0 : 1;
+            if (S < CHILD_GRID_MIN) {
+                CG_LAUNCH(KID_CHILDREN, 0,
+                          k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, wr, (uint32_t)L,
+                                                                B.segs[snext], B.list[0], B.P[0], trav_l, B.rs, sets,
+                                                                CHILD_ALL, B.blk));
+                return (int)COUPE_ERR_OK;
+            }
+            const unsigned g = (unsigned)((S + 1023) / 1024);
+            for (int ph : {(int)CHILD_COUNT, (int)CHILD_SCAN, (int)CHILD_WRITE}) {
+                CG_LAUNCH(KID_CHILDREN, 0,
+                          k_children<KT, WL><<<ph == CHILD_SCAN ? 1u : g, 1024, 0, s>>>(
+                              segs, (uint32_t)S, coord, D, wr, (uint32_t)L, B.segs[snext], B.list[0], B.P[0], trav_l,
+                              B.rs, sets, ph, B.blk));
+            }
             return (int)COUPE_ERR_OK;
         };
         const unsigned decide_grid = (unsigned)((S + NWARPS - 1) / NWARPS);

@@ -39,7 +39,7 @@ struct coupe_gpu_stats {
 	uint64_t max_split_steps; /* most steps of one split */
 	uint64_t hist_passes;     /* histogram passes launched */
 	uint64_t hist_points;     /* points read by histogram passes */
-	uint64_t band_points;     /* points re-checked in f64 (band mode) */
+	uint64_t band_points;     /* f64 coordinates read by histogram passes (band mode) */
 	uint64_t kernel_launches; /* kernels launched by the run */
 	uint64_t algo_bytes;      /* algorithmic HBM bytes of the run */
 	double root_weight_sum;   /* total weight as f64 */
