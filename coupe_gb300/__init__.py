@@ -19,7 +19,7 @@ import numpy as np
 
 __all__ = [
     "Rcb", "Rib", "CoupeError", "lib", "library_path", "MODES", "last_stats",
-    "rcb_device", "rib_device", "rib_matrix_device", "rcb_batched_device",
+    "rcb_device", "rib_device", "rib_matrix_device", "rcb_batched_device", "autotune_device",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -39,7 +39,7 @@ EXPORTED = [
     "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
-    "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched",
+    "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
 ]
 
 
@@ -58,6 +58,14 @@ class Stats(ctypes.Structure):
         "hist_points", "band_points", "kernel_launches", "algo_bytes")] + [
         ("root_weight_sum", ctypes.c_double), ("device_ms", ctypes.c_double),
         ("fixed_scale", ctypes.c_int), ("mode", ctypes.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("max_nbk", ctypes.c_int), ("hist_ctas_per_sm", ctypes.c_int),
+                ("reorder_chunks_per_cta", ctypes.c_int), ("device_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}
@@ -99,6 +107,8 @@ def lib():
     L.coupe_gpu_rib_device.restype = i32
     L.coupe_gpu_rcb_batched.argtypes = [vp, u64, vp, u64, vp, i32, vp, vp, dbl, i32, vp]
     L.coupe_gpu_rcb_batched.restype = i32
+    L.coupe_gpu_autotune.argtypes = [vp, u64, vp, u64, vp, i32, vp, vp, dbl, i32, vp, i32, ctypes.POINTER(Tuning)]
+    L.coupe_gpu_autotune.restype = i32
     L.coupe_gpu_rib_matrix.argtypes = [u64, u64, vp, vp, vp]
     L.coupe_gpu_rib_matrix.restype = i32
     L.coupe_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
@@ -272,6 +282,28 @@ def rcb_batched_device(part_ids, points, weights, set_offsets, iter_counts, tole
     rc = lib().coupe_gpu_rcb_batched(_ptr(part_ids), len(it), off.ctypes.data, dim, _ptr(points), wt,
                                      _ptr(weights), it.ctypes.data, tolerance, MODES[mode], ctypes.c_void_p(s))
     _check(rc)
+
+
+def autotune_device(part_ids, points, weights, set_offsets, iter_counts, tolerance, mode="ref32", repeats=2,
+                    stream=None):
+    """Times the batched call (arguments of rcb_batched_device) under each
+    candidate schedule and keeps the fastest process-wide; returns it as a
+    dict (max_nbk, hist_ctas_per_sm, reorder_chunks_per_cta, device_ms).
+    The ids never depend on the schedule."""
+    import torch
+    n, dim = points.shape
+    wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+    off = np.ascontiguousarray(np.asarray(set_offsets, dtype=np.uint64))
+    it = np.ascontiguousarray(np.asarray(iter_counts, dtype=np.uint32))
+    if off.ndim != 1 or it.ndim != 1 or len(off) != len(it) + 1 or int(off[-1]) != n:
+        raise ValueError("set_offsets must have len(iter_counts) + 1 entries ending at the number of points")
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    best = Tuning()
+    rc = lib().coupe_gpu_autotune(_ptr(part_ids), len(it), off.ctypes.data, dim, _ptr(points), wt, _ptr(weights),
+                                  it.ctypes.data, tolerance, MODES[mode], ctypes.c_void_p(s), int(repeats),
+                                  ctypes.byref(best))
+    _check(rc)
+    return best.as_dict()
 
 
 def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None):

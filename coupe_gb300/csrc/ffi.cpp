@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -473,6 +474,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "force_index_path")) return &t.force_index_path;
     if (!std::strcmp(name, "max_nbk")) return &t.max_nbk;
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
+    if (!std::strcmp(name, "hist_ctas_per_sm")) return &t.hist_ctas_per_sm;
     return nullptr;
 }
 
@@ -486,6 +488,53 @@ int coupe_gpu_set_option(const char *name, int64_t value) {
 int64_t coupe_gpu_get_option(const char *name) {
     int *p = option_slot(name);
     return p ? *p : -1;
+}
+
+enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const uint64_t *set_offsets,
+                                  uint64_t dimension, const double *d_points, enum coupe_type weight_type,
+                                  const void *d_weights, const uint32_t *iter_counts, double tolerance, int mode,
+                                  void *stream, int repeats, struct coupe_gpu_tuning *best) {
+    // Candidate schedules: bisection steps per histogram pass, histogram CTAs
+    // per SM and reorder chunks per CTA.  None changes the ids, so the
+    // fastest (median device time of `repeats` runs) is kept process-wide.
+    cg::Tuning &t = cg::tuning();
+    const cg::Tuning keep = t;
+    const int reps = repeats < 1 ? 1 : (repeats > 15 ? 15 : repeats);
+    double best_ms = 1e300;
+    cg::Tuning best_t = keep;
+    for (int nbk : {10, 9, 8})
+        for (int hc : {0, 3, 2})
+            for (int rc : {1, 2}) {
+                t = keep;
+                t.max_nbk = nbk;
+                t.hist_ctas_per_sm = hc;
+                t.reorder_chunks_per_cta = rc;
+                std::vector<double> ms;
+                for (int r = 0; r < reps + 1; ++r) {
+                    const coupe_err rc_ = coupe_gpu_rcb_batched(d_partition, nsets, set_offsets, dimension, d_points,
+                                                                weight_type, d_weights, iter_counts, tolerance, mode,
+                                                                stream);
+                    if (rc_ != COUPE_ERR_OK) {
+                        t = keep;
+                        return rc_;
+                    }
+                    if (r > 0) ms.push_back(t_stats.device_ms);  // the first run warms up
+                }
+                std::sort(ms.begin(), ms.end());
+                const double med = ms[ms.size() / 2];
+                if (med < best_ms) {
+                    best_ms = med;
+                    best_t = t;
+                }
+            }
+    t = best_t;
+    if (best) {
+        best->max_nbk = best_t.max_nbk;
+        best->hist_ctas_per_sm = best_t.hist_ctas_per_sm;
+        best->reorder_chunks_per_cta = best_t.reorder_chunks_per_cta;
+        best->device_ms = best_ms;
+    }
+    return COUPE_ERR_OK;
 }
 
 }  // extern "C"

@@ -725,6 +725,12 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     __shared__ uint64_t sw[HNB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
     __shared__ uint32_t scnt[HNB];
     __shared__ O sinv[HNB];
+    // band form: each warp's queue of items whose f64 coordinate is needed
+    // (offsets in the piece), drained 32 at a time, one item per lane, so
+    // that their dependent loads overlap instead of stalling every iteration
+    constexpr int SLOWQ = KT::BAND ? 64 : 1;
+    __shared__ uint32_t s_q[KT::BAND ? NWARPS : 1][SLOWQ];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int NB = 1 << nbk;
     int fs = L > 1 ? rs->fscale : 0;  // several sets: each set's own (set_fs)
     const bool packed = L == 1 && rs->wide == 0;
@@ -760,6 +766,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         uint64_t xcut = 0;
         uint64_t xm = ~0ull;  // band form: this thread's part of that minimum
         uint32_t nband = 0;   // band form: f64 coordinates this thread read
+        uint32_t qn = 0;      // band form: entries in this warp's queue (same in every lane)
         if constexpr (KT::BAND) {
             blo = band_bounds(lo);
             bhi = band_bounds(hi);
@@ -775,6 +782,44 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         O out_inv[2] = {0, 0};
 #pragma unroll
         for (int l = 0; l < L; ++l) out_w[0][l] = out_w[1][l] = 0;
+        // band form: one queued item (its key, weight and f64 coordinate)
+        auto band_item = [&](uint64_t e) {
+            if constexpr (KT::BAND) {
+                const K kk = keys[e];
+                const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
+                ++nband;
+                if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
+                uint64_t q[L];
+                WT::limbs(wts[e], fs, q);
+                const O v = (O)~KT::ord(kk);
+                const bool below = KeyF64::lt(c, lo), above = !below && !KeyF64::lt(c, hi);
+                if (below) {
+                    out_c[0] += 1;
+#pragma unroll
+                    for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
+                    out_inv[0] = v > out_inv[0] ? v : out_inv[0];
+                    return;
+                }
+                if (above) {
+                    out_c[1] += 1;
+#pragma unroll
+                    for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
+                    out_inv[1] = v > out_inv[1] ? v : out_inv[1];
+                    return;
+                }
+                bool unused;
+                const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cb_lo, cb_hi, NB, g, unused), c, cuts, NB);
+                if (packed) {
+                    atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+                } else {
+                    atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                    for (int l = 0; l < L; ++l)
+                        if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
+                }
+                if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+            }
+        };
         for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HIST_ITEMS) {
             K kv[HIST_ITEMS];
             typename WT::S wv[HIST_ITEMS];
@@ -838,43 +883,26 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                         if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
                     }
                 }
-                while (slow) {
-                    const int i = __ffs(slow) - 1;
-                    slow &= slow - 1;
-                    const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
-                    const K kk = keys[e];
-                    const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
-                    ++nband;
-                    if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
-                    uint64_t q[L];
-                    WT::limbs(wts[e], fs, q);
-                    const O v = (O)~KT::ord(kk);
-                    const bool below = KeyF64::lt(c, lo), above = !below && !KeyF64::lt(c, hi);
-                    if (below) {
-                        out_c[0] += 1;
-#pragma unroll
-                        for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
-                        out_inv[0] = v > out_inv[0] ? v : out_inv[0];
-                        continue;
+                if (__any_sync(0xffffffffu, slow != 0)) {
+#pragma unroll 1
+                    for (int i = 0; i < HIST_ITEMS; ++i) {
+                        const bool bit = (slow >> i) & 1u;
+                        const uint32_t m = __ballot_sync(0xffffffffu, bit);
+                        if (bit)
+                            s_q[warp][qn + __popc(m & ((1u << lane) - 1))] =
+                                (uint32_t)(base + (uint64_t)i * BLOCK + threadIdx.x - a);
+                        qn += __popc(m);
+                        if (qn >= 32) {
+                            __syncwarp();
+                            band_item(a + s_q[warp][lane]);
+                            // keep the rest (fewer than 32) at the front
+                            qn -= 32;
+                            const uint32_t v = lane < qn ? s_q[warp][32 + lane] : 0u;
+                            __syncwarp();
+                            if (lane < qn) s_q[warp][lane] = v;
+                        }
+                        __syncwarp();
                     }
-                    if (above) {
-                        out_c[1] += 1;
-#pragma unroll
-                        for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
-                        out_inv[1] = v > out_inv[1] ? v : out_inv[1];
-                        continue;
-                    }
-                    bool unused;
-                    const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cb_lo, cb_hi, NB, g, unused), c, cuts, NB);
-                    if (packed) {
-                        atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
-                    } else {
-                        atomicAdd(&scnt[bin], 1u);
-#pragma unroll
-                        for (int l = 0; l < L; ++l)
-                            if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
-                    }
-                    if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
                 }
                 continue;
             } else {
@@ -914,6 +942,12 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                     if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
                 }
             }
+            }
+        }
+        if constexpr (KT::BAND) {
+            if (qn) {
+                if (lane < qn) band_item(a + s_q[warp][lane]);  // the queue's rest
+                __syncwarp();
             }
         }
         if constexpr (KT::BAND) {

@@ -173,7 +173,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     const bool multi = R0.nsets > 1;
     const SetTab sets = B.set_tab(R0.nsets);
     const int32_t *set_fs = multi && WL::LIMBS > 1 ? B.set_fs : nullptr;
-    const int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
+    int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
+    if (tu.hist_ctas_per_sm > 0) g_hist = std::min(g_hist, tu.hist_ctas_per_sm * C.sms);
     if (multi) {
         CG_LAUNCH(KID_ROOT, 0,
                   k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,

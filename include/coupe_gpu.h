@@ -170,11 +170,33 @@ const char *coupe_gpu_kernel_name(int id);
  *                             reorder instead of tracing the recorded splits
  *   "max_nbk"                 bisection steps per histogram pass (1..10)
  *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
+ *   "hist_ctas_per_sm"        histogram CTAs per SM (0: as many as fit)
  * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
 int coupe_gpu_set_option(const char *name, int64_t value);
 
 /* Current value of a knob, or -1 for an unknown name. */
 int64_t coupe_gpu_get_option(const char *name);
+
+/* The schedule coupe_gpu_autotune chose. */
+struct coupe_gpu_tuning {
+	int max_nbk;
+	int hist_ctas_per_sm;
+	int reorder_chunks_per_cta;
+	double device_ms; /* median device time of the chosen schedule */
+};
+
+/* Autotuner (no counterpart in the reference): runs the batched call of
+ * coupe_gpu_rcb_batched (same arguments; nsets = 1 for one set) under each
+ * candidate schedule of the knobs above, `repeats` timed runs each after one
+ * warm-up, and keeps the fastest process-wide (the ids are the same under
+ * every schedule).  `best` (may be NULL) receives the choice; d_partition
+ * holds the ids of the last run.  18 candidates: budget about
+ * 18 * (repeats + 1) runs of the workload. */
+enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets,
+		const uint64_t *set_offsets, uint64_t dimension, const double *d_points,
+		enum coupe_type weight_type, const void *d_weights,
+		const uint32_t *iter_counts, double tolerance, int mode, void *stream,
+		int repeats, struct coupe_gpu_tuning *best);
 
 /* Library version string. */
 const char *coupe_gpu_version(void);

@@ -129,3 +129,29 @@ def test_batched_matches_after_other_sizes(coupe, oracle_mod):
         pts, w, off, it = _sets(rng, sizes, 3, "i64", iters)
         want = oracle_mod.rcb_sets(pts, w, off, it, 0.01, threads=0)
         assert np.array_equal(want, _gpu(coupe, torch, pts, w, off, it, 0.01, "ref32"))
+
+
+def test_autotune_keeps_ids(coupe, oracle_mod):
+    """The autotuner picks one of its candidate schedules; the ids under it
+    are those of the default schedule (and of the oracle)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    sizes = [int(x) for x in rng.integers(5_000, 300_000, 30)]
+    iters = rng.integers(1, 9, len(sizes))
+    pts, w, off, it = _sets(rng, sizes, 3, "i64", iters)
+    want = oracle_mod.rcb_sets(pts, w, off, it, 0.01, mode=1, threads=0)
+    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta")
+    keep = {k: coupe.get_option(k) for k in names}
+    try:
+        dp = torch.from_numpy(pts).cuda()
+        dw = torch.from_numpy(w).cuda()
+        ids = torch.zeros(len(pts), dtype=torch.int64, device="cuda")
+        best = coupe.autotune_device(ids, dp, dw, off, it, 0.01, mode="f32key_f64band", repeats=1)
+        assert best["max_nbk"] in (8, 9, 10) and best["hist_ctas_per_sm"] in (0, 2, 3)
+        assert best["reorder_chunks_per_cta"] in (1, 2) and best["device_ms"] > 0
+        assert {k: coupe.get_option(k) for k in names} == {k: best[k] for k in names}
+        assert np.array_equal(ids.cpu().numpy().astype(np.uint64), want)
+        assert np.array_equal(_gpu(coupe, torch, pts, w, off, it, 0.01, "f32key_f64band"), want)
+    finally:
+        for k, v in keep.items():
+            coupe.set_option(k, v)

@@ -288,7 +288,8 @@ def test_rib_end_to_end(coupe, oracle_mod):
 @pytest.mark.parametrize("knobs", [{"force_index_path": 1}, {"max_nbk": 3}, {"max_nbk": 1}, {"max_nbk": 8},
                                    {"reorder_chunks_per_cta": 4}, {"reorder_chunks_per_cta": 64},
                                    {"max_nbk": 5, "reorder_chunks_per_cta": 3},
-                                   {"force_index_path": 1, "reorder_chunks_per_cta": 7}])
+                                   {"force_index_path": 1, "reorder_chunks_per_cta": 7},
+                                   {"hist_ctas_per_sm": 1}, {"hist_ctas_per_sm": 2, "max_nbk": 9}])
 def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     """Part ids through the index path, fewer bisection steps per pass and
     other chunkings equal the oracle's."""
