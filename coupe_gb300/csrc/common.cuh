@@ -461,12 +461,26 @@ struct Seg {
     uint32_t xstate; // band form: X_PENDING when xmin holds an exact minimum
     uint32_t xkey;   // band form: the f32 key (ordered) whose exact minimum xmin is
     uint32_t set;    // point set of the run the segment belongs to
+    // f64 weights binned approximately (see k_hist): the exact sums come
+    // from xq, the segment's own fixed-point sum (chunks of 32 bits, summed
+    // by the level's first pass)
+    uint32_t sumx;    // SUMX_*: how the first decide pass of the level sets `sum`
+    uint32_t exactw;  // 1: the next passes bin exact fixed-point weights
+    uint32_t wlx;     // 1: wl is exact (set with a split)
+    uint32_t pad2;
+    uint64_t xq[4];
     uint64_t xcut;   // band form: ... among the items at or right of this cut
     uint64_t xmin;   // band form: that minimum (f64 ordered code)
     K lo, hi;        // current search interval on this level's axis
     K pivot;         // result: items with key < pivot go left
     K split_pos;     // result: the cut position
     K bmin[3], bmax[3];
+};
+
+enum : uint32_t {
+    SUMX_NONE = 0,   // sum is exact
+    SUMX_OWN = 1,    // sum = the items' own fixed-point sum (a left child)
+    SUMX_RIGHT = 2,  // sum = parent sum - left sibling's (segment index - 1) own sum
 };
 
 // One finished split as the final traversal needs it: items with
@@ -500,6 +514,7 @@ struct SetTab {
     uint64_t *wsum;         // [count * 4] weight sum limbs
     uint64_t *wabs;         // [count] largest |w| as raw f64 bits (f64 weights)
     int32_t *fs;            // [count] fixed-point scale (f64 weights)
+    int32_t *qb;            // [count] shift of the approximate binned weights (f64 weights)
     uint64_t *minheap;      // [count] smallest heap id among the set's parts
 };
 
@@ -536,6 +551,10 @@ struct RunScalars {
     uint32_t pad2;
     unsigned long long band_points;  // band form: f64 coordinates read
     uint64_t items_next;             // items of the next level's segments
+    uint32_t fneg;                   // f64 weights: some weight is negative
+    int32_t qb;                      // f64 weights, one set: shift of the approximate binned weights
+    uint32_t fapprox;                // f64 weights: bins hold approximate weights (see k_hist)
+    uint32_t nexactw;                // decisions that needed exact f64 weight sums
 };
 
 }  // namespace cg

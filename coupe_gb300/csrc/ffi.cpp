@@ -475,6 +475,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "max_nbk")) return &t.max_nbk;
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
     if (!std::strcmp(name, "hist_ctas_per_sm")) return &t.hist_ctas_per_sm;
+    if (!std::strcmp(name, "exact_f64_hist")) return &t.exact_f64_hist;
     return nullptr;
 }
 

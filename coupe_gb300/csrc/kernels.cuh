@@ -416,14 +416,19 @@ static __global__ void __launch_bounds__(BLOCK) k_wabs_max(const double *__restr
     if ((threadIdx.x & 31) == 0) atomicMax((unsigned long long *)&rs->wabs_max_bits, (unsigned long long)m);
 }
 
+// Shift of the approximate binned weights of a set of n items: its
+// fixed-point weights are below 2^(126 - ceil(log2 n)), so q >> shift < 2^25.
+__device__ __forceinline__ int approx_shift(uint64_t n) { return 101 - ceil_log2_u64(n); }
+
 // Several sets, f64 weights: each set's fixed-point scale (from its own
 // largest |w| and size, as a run of that set alone chooses it).
 static __global__ void k_set_fs(SetTab sets, RunScalars *rs) {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= sets.count) return;
-    const uint64_t b = sets.wabs[s];
+    const uint64_t b = sets.wabs[s], n = sets.off[s + 1] - sets.off[s];
     if (b >= 0x7ff0000000000000ull) atomicOr(&rs->err, ERR_NONFINITE_WEIGHT);
-    sets.fs[s] = fixed_scale_from_max(__longlong_as_double((long long)b), sets.off[s + 1] - sets.off[s]);
+    sets.fs[s] = fixed_scale_from_max(__longlong_as_double((long long)b), n);
+    sets.qb[s] = approx_shift(n);
 }
 
 __device__ __forceinline__ int run_fscale(const RunScalars *rs, uint64_t n) {
@@ -439,7 +444,7 @@ __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict
     uint64_t acc[WT::LIMBS];
 #pragma unroll
     for (int l = 0; l < WT::LIMBS; ++l) acc[l] = 0;
-    bool wide = WT::LIMBS > 1, not16 = false;
+    bool wide = WT::LIMBS > 1, not16 = false, neg = false;
     // several sets: one contiguous range per CTA; a thread's sum goes to its
     // set whenever its items enter another set
     uint64_t i0 = (uint64_t)blockIdx.x * BLOCK + threadIdx.x, i1 = n, step = (uint64_t)gridDim.x * BLOCK;
@@ -469,7 +474,9 @@ __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict
         WT::limbs(wi, fs, q);
 #pragma unroll
         for (int l = 0; l < WT::LIMBS; ++l) acc[l] += q[l];
-        if constexpr (WT::LIMBS == 1) {
+        if constexpr (WT::LIMBS > 1) {
+            neg |= wi < 0;
+        } else {
             wide |= !(wi >= 0 && wi < (1 << PACK_WBITS_IN));
             if (c16) {
                 // the 16-bit copy of the level loop, used when no weight fails
@@ -480,6 +487,7 @@ __global__ void __launch_bounds__(BLOCK) k_wsum(const typename WT::S *__restrict
     }
     if (__any_sync(0xffffffffu, not16) && (threadIdx.x & 31) == 0) atomicOr(&rs->narrow16, 1u);
     if (__any_sync(0xffffffffu, wide) && (threadIdx.x & 31) == 0) atomicOr(&rs->wide, 1u);
+    if (__any_sync(0xffffffffu, neg) && (threadIdx.x & 31) == 0) atomicOr(&rs->fneg, 1u);
     if (multi) {
         flush();
         return;
@@ -511,6 +519,11 @@ __device__ Seg<KT> root_seg(uint64_t off, uint64_t voff, uint64_t n, uint32_t se
     s.xstate = 0;
     s.xkey = 0;
     s.set = set;
+    s.sumx = SUMX_NONE;
+    s.exactw = 0;
+    s.wlx = 0;
+    s.pad2 = 0;
+    for (int l = 0; l < 4; ++l) s.xq[l] = 0;
     s.xcut = 0;
     s.xmin = ~0ull;
     for (int d = 0; d < 3; ++d) {
@@ -528,9 +541,12 @@ __device__ Seg<KT> root_seg(uint64_t off, uint64_t voff, uint64_t n, uint32_t se
 
 // Root segment of a one-set run.
 template <class KT, class WT>
-__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs) {
+__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs, int approx) {
     const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
     rs->fscale = fs;
+    rs->qb = approx_shift(n);
+    // approximate bins need non-negative fixed-point weights
+    rs->fapprox = WT::LIMBS > 1 && approx && rs->fneg == 0;
     if (WT::LIMBS > 1 && rs->wabs_max_bits >= 0x7ff0000000000000ull) rs->err |= ERR_NONFINITE_WEIGHT;
     segs[0] = root_seg<KT, WT>(0, 0, n, 0, rs->wsum_limbs, fs, rs->bbox_min_ord, rs->bbox_max_ord, D);
     list[0] = 0;
@@ -542,8 +558,9 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
 // P[r] in the level's list of items (P written by the host).
 template <class KT, class WT>
 __global__ void k_roots(Seg<KT> *segs, uint32_t *list, const uint64_t *P, const uint32_t *roots, uint32_t nroots,
-                        int D, SetTab sets) {
+                        int D, SetTab sets, RunScalars *rs, int approx) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0) rs->fapprox = WT::LIMBS > 1 && approx && rs->fneg == 0;
     if (r >= nroots) return;
     const uint32_t st = roots[r];
     const int fs = WT::LIMBS > 1 ? sets.fs[st] : 0;
@@ -563,6 +580,7 @@ static __global__ void k_sets_init(SetTab sets) {
     for (int l = 0; l < 4; ++l) sets.wsum[s * 4 + l] = 0;
     sets.wabs[s] = 0;
     sets.fs[s] = 0;
+    sets.qb[s] = 0;
     sets.minheap[s] = ~0ull;
 }
 
@@ -713,7 +731,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
                                                 uint64_t n_total, const RunScalars *rs, int nlist_dev,
                                                 const uint32_t *__restrict__ isrc, BandSrc bs, int coord,
-                                                Seg<KT> *segs_w, const int32_t *__restrict__ set_fs) {
+                                                Seg<KT> *segs_w, const int32_t *__restrict__ set_fs,
+                                                const int32_t *__restrict__ set_qb) {
     typedef typename KT::T K;
     typedef typename KT::C CK;
     typedef typename KT::Ord O;
@@ -733,7 +752,9 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int NB = 1 << nbk;
     int fs = L > 1 ? rs->fscale : 0;  // several sets: each set's own (set_fs)
-    const bool packed = L == 1 && rs->wide == 0;
+    int qb = L > 1 ? rs->qb : 0;      // several sets: each set's own (set_qb)
+    const bool packed_all = L == 1 && rs->wide == 0;
+    const bool fapprox = L > 1 && rs->fapprox != 0;
     if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass: the list the last scan left
     const uint64_t T = P[nlist];
     const uint64_t c0 = T * blockIdx.x / gridDim.x, c1 = T * (blockIdx.x + 1) / gridDim.x;
@@ -745,7 +766,46 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         const uint32_t s = list[k];
         const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
         const Seg<KT> &sg = segs[s];
-        if (L > 1 && set_fs) fs = set_fs[sg.set];
+        if (L > 1 && set_fs) {
+            fs = set_fs[sg.set];
+            qb = set_qb[sg.set];
+        }
+        // f64 weights: unless this segment's decisions asked for exact bins,
+        // a bin holds the count and the sum of floor(q / 2^qb) of its items
+        // (q: an item's fixed-point weight, below 2^(126 - ceil(log2 n)), so
+        // floor(q / 2^qb) < 2^25 and 2^19 of them fit the packed 44 bits);
+        // the decisions bound the exact sums from these.  The level's first
+        // pass also sums the segment's exact q (every item, NaN keys too):
+        // the segment's weight sum when it is a left child.
+        const bool apx = fapprox && sg.exactw == 0;
+        const bool packed = packed_all || apx;
+        const bool accx = L > 1 && sg.sumx != SUMX_NONE;
+        uint64_t xacc[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) xacc[l] = 0;
+        auto item_q = [&](typename WT::S w, uint64_t *q) {
+            if constexpr (L > 1) {
+                const unsigned __int128 qq = fixed_q_bits((double)w, fs);
+                if (accx) {
+                    xacc[0] += (uint32_t)qq;
+                    xacc[1] += (uint32_t)(qq >> 32);
+                    xacc[2] += (uint32_t)(qq >> 64);
+                    xacc[3] += (uint32_t)(qq >> 96);
+                }
+                if (apx) {
+                    q[0] = (uint64_t)(qq >> qb);
+#pragma unroll
+                    for (int l = 1; l < L; ++l) q[l] = 0;
+                } else {
+                    q[0] = (uint32_t)qq;
+                    q[1] = (uint32_t)(qq >> 32);
+                    q[2] = (uint32_t)(qq >> 64);
+                    q[3] = (uint32_t)(qq >> 96);
+                }
+            } else {
+                WT::limbs(w, fs, q);
+            }
+        };
         const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
         const CK lo = sg.lo, hi = sg.hi;
         __syncthreads();
@@ -790,7 +850,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                 ++nband;
                 if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
                 uint64_t q[L];
-                WT::limbs(wts[e], fs, q);
+                item_q(wts[e], q);
                 const O v = (O)~KT::ord(kk);
                 const bool below = KeyF64::lt(c, lo), above = !below && !KeyF64::lt(c, hi);
                 if (below) {
@@ -841,6 +901,10 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
 #pragma unroll
                 for (int i = 0; i < HIST_ITEMS; ++i) {
                     const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                    if (L > 1 && accx && e < b && KT::isnan(kv[i])) {
+                        uint64_t q[L];
+                        item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
+                    }
                     if (e < b && !KT::isnan(kv[i])) {
                         if (xpend && KT::ord(kv[i]) == xkey) {
                             slow |= 1u << i;
@@ -855,7 +919,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                             continue;
                         }
                         uint64_t q[L];
-                        WT::limbs(wv[i], fs, q);
+                        item_q(wv[i], q);
                         const O v = (O)~KT::ord(kv[i]);
                         if (sl < 0 || sh > 0) {
                             // constant indices only: keeps the sums in registers
@@ -909,9 +973,13 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
 #pragma unroll
             for (int i = 0; i < HIST_ITEMS; ++i) {
                 const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
+                if (L > 1 && accx && e < b && KT::isnan(kv[i])) {
+                    uint64_t q[L];
+                    item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
+                }
                 if (e < b && !KT::isnan(kv[i])) {
                     uint64_t q[L];
-                    WT::limbs(wv[i], fs, q);
+                    item_q(wv[i], q);
                     const bool below = KT::lt(kv[i], lo), above = !below && !KT::lt(kv[i], hi);
                     if (below || above) {
                         // constant indices only: keeps the sums in registers
@@ -948,6 +1016,15 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             if (qn) {
                 if (lane < qn) band_item(a + s_q[warp][lane]);  // the queue's rest
                 __syncwarp();
+            }
+        }
+        if constexpr (L > 1) {
+            if (accx) {
+#pragma unroll
+                for (int l = 0; l < L; ++l) {
+                    const uint64_t v = warp_sum_u64(xacc[l]);
+                    if ((threadIdx.x & 31) == 0 && v) atomicAdd((unsigned long long *)&segs_w[s].xq[l], (unsigned long long)v);
+                }
             }
         }
         if constexpr (KT::BAND) {
@@ -988,6 +1065,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             if (packed) {
                 c = (uint32_t)(sw[i] >> PACK_SHIFT);
                 wl[0] = sw[i] & PACK_WMASK;
+#pragma unroll
+                for (int l = 1; l < L; ++l) wl[l] = 0;
             } else {
                 c = scnt[i];
 #pragma unroll
@@ -1015,7 +1094,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
 template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
-                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs) {
+                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs,
+                                                  const int32_t *__restrict__ set_qb) {
     typedef typename KT::C K;  // cuts and interval bounds
     typedef typename KT::Ord O;
     typedef typename WT::V V;
@@ -1034,6 +1114,9 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     // narrower than a block, the one block left is spread over the lanes.
     const int BS = NB >= 32 ? NB / 32 : 1;
     const int fs = L > 1 ? (set_fs ? set_fs[sg.set] : rs->fscale) : 0;
+    const int qb = L > 1 ? (set_qb ? set_qb[sg.set] : rs->qb) : 0;
+    // f64 weights: bins of truncated weights (k_hist) unless exact ones were asked for
+    const bool apx = L > 1 && rs->fapprox != 0 && sg.exactw == 0;
     const size_t g0 = (size_t)s * NB;
     auto load_bin = [&](int b, uint64_t &c, uint64_t *w, O &m) {
         const size_t g = g0 + b;
@@ -1078,7 +1161,16 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 #pragma unroll
     for (int l = 0; l < L; ++l) Fw[l] = 0;
 
-    const V sum = WT::from_bits(sg.sum);
+    // the level's first decisions settle a child's sum from exact sums of
+    // the first pass: coupe's weight_left for a left child, sum - weight_left
+    // for a right one (recursive_bisection.rs:606-641)
+    V sum = WT::from_bits(sg.sum);
+    if constexpr (L > 1) {
+        if (sg.sumx == SUMX_OWN)
+            sum = WT::value(sg.xq, fs);
+        else if (sg.sumx == SUMX_RIGHT)
+            sum = WT::sub(sum, WT::value(segs[s - 1].xq, fs));
+    }
     K lo = sg.lo, hi = sg.hi;
     uint64_t prev = sg.prev;
     int lo_b = 0, hi_b = NB;
@@ -1088,12 +1180,14 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     for (int l = 0; l < L; ++l) w_below[l] = 0;
     O kmin_above = NONE;
     bool flag_exact = false;  // band form: a test needs an exact minimum first
+    bool flag_exactw = false;  // f64 weights: a test needs exact bins first
     K xcut = 0;
     O xkey = 0;
     uint32_t state = SEG_ACTIVE;
     uint32_t steps = 0;
     K pivot = 0, split_pos = 0;
     V wl_out = 0;
+    bool wl_exact = true;
     uint64_t nleft = 0;
     for (int step = 0; step < nbk; ++step) {
         const int mid_b = (lo_b + hi_b) >> 1;
@@ -1171,21 +1265,51 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
                 atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // its resolution found no item
             break;
         }
-        const V wl = WT::value(wacc, fs);
+        // weight_left: exact, or with truncated bins the interval
+        // [A 2^qb, A 2^qb + count (2^qb - 1)] of its fixed-point value
+        V wl = WT::value(wacc, fs), wl_hi = wl;
+        if constexpr (L > 1) {
+            if (apx) {
+                const unsigned __int128 ql = (unsigned __int128)wacc[0] << qb;
+                wl = fixed_to_f64(ql, fs);
+                wl_hi = fixed_to_f64(ql + (unsigned __int128)count * ((((unsigned __int128)1) << qb) - 1), fs);
+            }
+        }
         const double ideal = WT::f64(sum) / 2.0;
-        const double imb = fabs((WT::f64(wl) - ideal) / ideal);
-        // recursive_bisection.rs:547-563; `hi <= t + dist` is monotone in dist
+        // recursive_bisection.rs:547-563.  imbalance <= tol holds on an
+        // interval of weight_left values that contains sum/2 (f64 rounding is
+        // monotone), so two ends that agree settle it, unless both fail on
+        // either side of sum/2; `hi <= t + dist` is monotone in dist.
+        const bool p_lo = fabs((WT::f64(wl) - ideal) / ideal) <= tol;
+        const bool p_hi = fabs((WT::f64(wl_hi) - ideal) / ideal) <= tol;
+        const bool spans = ideal != 0.0 && WT::f64(wl) <= ideal && ideal <= WT::f64(wl_hi);
+        const bool imb_yes = p_lo && p_hi, imb_no = !p_lo && !p_hi && !(spans && tol >= 0.0);
         const bool near_lo = hv <= tv + dl, near_hi = hv <= tv + dh;
-        if (!(count == prev || imb <= tol) && near_lo != near_hi) {
-            flag_exact = true;
-            --steps;
-            xcut = t;
-            xkey = kminO;
-            if (sg.xstate == X_PENDING && sg.xcut == t && sg.xkey == (uint32_t)kminO && lane == 0)
-                atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // its resolution found no item
+        const bool stop = count == prev || near_lo || imb_yes;
+        bool need_x = false, need_w = false;
+        if (!stop) {
+            need_x = near_hi;  // band form: only the exact minimum tells
+            need_w = !imb_no;
+            // coupe's update (:564-571) is monotone in weight_left
+            if (!need_x && !need_w && WT::less(wl, WT::sub(sum, wl)) != WT::less(wl_hi, WT::sub(sum, wl_hi)))
+                need_w = true;
+        }
+        if (need_x || need_w) {
+            --steps;  // this step is replayed once its inputs are exact
+            if (need_x) {
+                flag_exact = true;
+                xcut = t;
+                xkey = kminO;
+                if (sg.xstate == X_PENDING && sg.xcut == t && sg.xkey == (uint32_t)kminO && lane == 0)
+                    atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // its resolution found no item
+            }
+            if (need_w) {
+                flag_exactw = true;
+                if (!apx && lane == 0) atomicOr(&rs->err, ERR_COUNT_MISMATCH);  // exact bins cannot be undecided
+            }
             break;
         }
-        if (count == prev || near_lo || imb <= tol) {
+        if (stop) {
             state = SEG_DONE;
             // items with key < pivot go left; in the band form the cut itself
             // (no item lies in [t, min right), so x < t is the same set)
@@ -1195,6 +1319,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
                 pivot = KT::unord(kminO);
             split_pos = t;
             wl_out = wl;
+            wl_exact = !apx;
             nleft = count;
             break;
         }
@@ -1219,6 +1344,11 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             o.pivot = pivot;
             o.split_pos = split_pos;
             o.wl = WT::bits(wl_out);
+            o.wlx = wl_exact ? 1u : 0u;
+            if (L > 1 && sg.sumx != SUMX_NONE) {
+                o.sum = WT::bits(sum);
+                o.sumx = SUMX_NONE;
+            }
             o.nleft = (uint32_t)nleft;
             o.steps = total_steps;
             o.lo = lo;
@@ -1245,6 +1375,14 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             o.hi = hi;
             o.prev = prev;
             o.steps = total_steps;
+            if (L > 1 && sg.sumx != SUMX_NONE) {
+                o.sum = WT::bits(sum);
+                o.sumx = SUMX_NONE;
+            }
+            if (flag_exactw) {
+                o.exactw = 1;
+                atomicAdd(&rs->nexactw, 1u);
+            }
             if (KT::BAND && flag_exact) {
                 o.xstate = X_PENDING;
                 o.xcut = xcut;
@@ -1415,7 +1553,20 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
                     ch.off = side == 0 ? sg.off : sg.off + nl;
                     ch.voff = outv + vi + (side == 0 ? 0 : nl);
                     ch.heap = side == 0 ? hl : hr;
-                    ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
+                    if (sg.wlx) {
+                        ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
+                        ch.sumx = SUMX_NONE;
+                    } else {
+                        // weight_left known only within bounds: the next
+                        // level's first pass sums the left child's items
+                        ch.sum = side == 0 ? 0 : sg.sum;
+                        ch.sumx = side == 0 ? SUMX_OWN : (nl > 0 ? SUMX_RIGHT : SUMX_NONE);
+                    }
+                    ch.exactw = 0;
+                    ch.wlx = 0;
+                    ch.pad2 = 0;
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) ch.xq[l] = 0;
                     ch.prev = ~0ull;
                     ch.wl = 0;
                     ch.n = cn;

@@ -66,7 +66,7 @@ struct Buffers {
     // several sets: the set table and the sets of the root segments
     uint64_t *set_off, *set_bmin, *set_bmax, *set_wsum, *set_wabs, *set_minheap;
     uint32_t *set_iters, *set_root, *roots;
-    int32_t *set_fs;
+    int32_t *set_fs, *set_qb;
 
     SetTab set_tab(uint32_t count) const {
         SetTab t;
@@ -79,6 +79,7 @@ struct Buffers {
         t.wsum = set_wsum;
         t.wabs = set_wabs;
         t.fs = set_fs;
+        t.qb = set_qb;
         t.minheap = set_minheap;
         return t;
     }
@@ -105,7 +106,7 @@ struct Buffers {
         hist_bins = hb;
         set_off = set_bmin = set_bmax = set_wsum = set_wabs = set_minheap = nullptr;
         set_iters = set_root = roots = nullptr;
-        set_fs = nullptr;
+        set_fs = set_qb = nullptr;
         if (nsets) {
             set_off = b.take<uint64_t>(nsets + 1);
             set_iters = b.take<uint32_t>(nsets);
@@ -116,6 +117,7 @@ struct Buffers {
             set_wsum = b.take<uint64_t>(nsets * 4);
             set_wabs = b.take<uint64_t>(nsets);
             set_fs = b.take<int32_t>(nsets);
+            set_qb = b.take<int32_t>(nsets);
             set_minheap = b.take<uint64_t>(nsets);
         }
         return b.off;
@@ -173,14 +175,16 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     const bool multi = R0.nsets > 1;
     const SetTab sets = B.set_tab(R0.nsets);
     const int32_t *set_fs = multi && WL::LIMBS > 1 ? B.set_fs : nullptr;
+    const int32_t *set_qb = multi && WL::LIMBS > 1 ? B.set_qb : nullptr;
+    const int approx = tu.exact_f64_hist ? 0 : 1;
     int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
     if (tu.hist_ctas_per_sm > 0) g_hist = std::min(g_hist, tu.hist_ctas_per_sm * C.sms);
     if (multi) {
         CG_LAUNCH(KID_ROOT, 0,
                   k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,
-                                                                           R0.nroots, D, sets));
+                                                                           R0.nroots, D, sets, B.rs, approx));
     } else {
-        CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs));
+        CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs, approx));
     }
     const uint64_t sk = sizeof(K), sw = sizeof(WS), si = carry ? 4 : 0;
 
@@ -244,13 +248,13 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
         CG_LAUNCH(KID_HIST, V * (sk + sw),
                   k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], (uint32_t)S, kc, wc, H, nbk, n,
-                                                          B.rs, 0, hsrc, bs, coord, segs, set_fs));
+                                                          B.rs, 0, hsrc, bs, coord, segs, set_fs, set_qb));
         ++st->hist_passes;
         st->hist_points += V;
         bytes += V * (sk + sw);
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
-                                                                 B.flags, B.rs, 0, set_fs));
+                                                                 B.flags, B.rs, 0, set_fs, set_qb));
         CG_LAUNCH(KID_SCAN, 0,
                   k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[0], B.flags, (uint32_t)S, B.list[1], B.P[1], B.rs, 0));
         // A speculative second pass over list[1] without asking the host how
@@ -258,11 +262,11 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         // once when no segment is searching.  The next scan leaves list[0].
         CG_LAUNCH(KID_HIST, 0,
                   k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1, hsrc,
-                                                          bs, coord, segs, set_fs));
+                                                          bs, coord, segs, set_fs, set_qb));
         ++st->hist_passes;
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
-                                                                 B.rs, 1, set_fs));
+                                                                 B.rs, 1, set_fs, set_qb));
         CG_LAUNCH(KID_SCAN, 0,
                   k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[1], B.flags, 0, B.list[0], B.P[0], B.rs, 1));
         // k_children returns at once if a segment is still searching
@@ -289,11 +293,11 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             const uint64_t nlist = h_rs->nactive;
             CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
                       k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs, set_fs));
+                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs, set_fs, set_qb));
             ++st->hist_passes;
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
-                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs));
+                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs, set_qb));
             CG_LAUNCH(KID_SCAN, 0,
                       k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
                                                          B.P[li ^ 1], B.rs, 0));
@@ -412,6 +416,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     bytes += h_rs->pass_points * (sk + sw);
     st->algo_bytes = bytes;
     st->band_points = h_rs->band_points;
+    st->weight_rechecks = h_rs->nexactw;
     if (h_rs->err) {
         uint32_t e = h_rs->err;
         if (e & ERR_NONFINITE_WEIGHT) {

@@ -46,6 +46,7 @@ struct coupe_gpu_stats {
 	double device_ms;         /* device time of the run (CUDA events) */
 	int fixed_scale;          /* s of the 128-bit fixed-point weight sums */
 	int mode;                 /* enum coupe_gpu_mode used */
+	uint64_t weight_rechecks; /* f64 weights: decisions replayed with exact bins */
 };
 
 /* coupe_rcb with an explicit precision mode. */
@@ -171,6 +172,10 @@ const char *coupe_gpu_kernel_name(int id);
  *   "max_nbk"                 bisection steps per histogram pass (1..10)
  *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
  *   "hist_ctas_per_sm"        histogram CTAs per SM (0: as many as fit)
+ *   "exact_f64_hist"          1: bin f64 weights as exact fixed-point sums in
+ *                             every pass (by default the bins hold truncated
+ *                             sums and a decision they cannot settle is
+ *                             replayed from exact bins)
  * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
 int coupe_gpu_set_option(const char *name, int64_t value);
 

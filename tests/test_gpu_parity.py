@@ -392,3 +392,53 @@ def test_key_conversion_is_ieee_rne(coupe):
     nan = np.isnan(want)
     assert (np.isnan(got) == nan).all()
     assert (got[~nan].view(np.uint32) == want[~nan].view(np.uint32)).all()
+
+
+# ---------------------------------------------------------------------------
+# f64 weights: bins of truncated fixed-point weights, exact replays
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
+def test_f64_weights_exact_bins_equal_truncated_bins(coupe, oracle_mod, mode):
+    """The f64 random cases with the histograms forced to exact fixed-point
+    sums give the same ids as the default truncated bins (and the oracle)."""
+    cases = [c for c in CASES if c[2] == "f64"]
+    try:
+        for n, dim, wk, iters, tol, seed in cases:
+            pts, w = _make(n, dim, wk, seed)
+            want, _ = oracle_mod.rcb(pts, w, iters, tol, mode=_oracle_mode(mode))
+            coupe.set_option("exact_f64_hist", 1)
+            exact = _gpu(coupe, pts, w, iters, tol, mode=mode)
+            assert coupe.last_stats()["weight_rechecks"] == 0
+            coupe.set_option("exact_f64_hist", 0)
+            trunc = _gpu(coupe, pts, w, iters, tol, mode=mode)
+            assert np.array_equal(exact, want) and np.array_equal(trunc, want), (n, dim, iters)
+    finally:
+        coupe.set_option("exact_f64_hist", 0)
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f32key_f64band"])
+@pytest.mark.parametrize("tol", [0.0, 1e-7])
+def test_f64_weights_undecided_steps_replay_exactly(coupe, oracle_mod, mode, tol):
+    """Tolerances 0 and 1e-7: weight_left is compared with sum/2 closer than
+    the truncated bins can tell, so splits replay steps from exact bins
+    (weight_rechecks > 0); the ids still equal the oracle's."""
+    rng = np.random.default_rng(77)
+    n = 300_000
+    pts = rng.random((n, 3))
+    w = rng.lognormal(0.0, 2.0, n)
+    want, _ = oracle_mod.rcb(pts, w, 8, tol, mode=_oracle_mode(mode))
+    got = _gpu(coupe, pts, w, 8, tol, mode=mode)
+    assert coupe.last_stats()["weight_rechecks"] > 0
+    assert np.array_equal(got, want)
+
+
+def test_f64_weights_negative_use_exact_bins(coupe, oracle_mod):
+    """Negative f64 weights have no truncated bins (every pass is exact)."""
+    rng = np.random.default_rng(78)
+    pts = rng.random((200_000, 2))
+    w = rng.normal(1.0, 3.0, len(pts))
+    for mode, om in (("f64", 1), ("f32key_f64band", 1), ("ref32", 0)):
+        want, _ = oracle_mod.rcb(pts, w, 7, 0.01, mode=om)
+        got = _gpu(coupe, pts, w, 7, 0.01, mode=mode)
+        assert coupe.last_stats()["weight_rechecks"] == 0
+        assert np.array_equal(got, want)
