@@ -1635,19 +1635,27 @@ struct ReorderArgs {
     typename WT::S *wdst;
     const uint32_t *isrc;  // NULL: identity
     uint32_t *idst;
+    int wsafe;     // 1: wsrc is an engine buffer (tiles copied in 16-byte chunks)
     uint64_t *lb;  // look-back words, one per chunk, zeroed
     RunScalars *rs;
     BandSrc bs;    // band form: the f64 coordinates (through isrc)
 };
 
-// One tile in shared memory: D key tiles and a weight tile (16 bytes of
-// slack: 16-bit weights arrive as the 4-byte words covering the tile).
-// Carried input indices are not double buffered: each thread loads its own
-// items' indices into registers when the tile starts (overlapping the
-// partition work) and parks them in one shared array for the output loop.
+// One tile in shared memory: D key arrays and a weight array, each with 16
+// bytes of slack.  Arrays in engine buffers (keys, and weights after level 0)
+// arrive as the 16-byte chunks covering the tile, starting at the aligned
+// address at or below it; element li of the tile is then at li + head, head =
+// ts mod (16 / element size).  Carried input indices are not double
+// buffered: each thread loads its own items' indices into registers when the
+// tile starts (overlapping the partition work) and parks them in one shared
+// array for the output loop.
+template <int D, class KT>
+__host__ __device__ constexpr size_t reorder_key_stride() {
+    return (size_t)R_TILE * sizeof(typename KT::T) + 16;
+}
 template <int D, class KT, class WT>
 __host__ __device__ constexpr size_t reorder_tile_bytes() {
-    return (size_t)R_TILE * (D * sizeof(typename KT::T) + sizeof(typename WT::S)) + 16;
+    return D * reorder_key_stride<D, KT>() + (size_t)R_TILE * sizeof(typename WT::S) + 16;
 }
 
 // Dynamic shared memory of the reorder: two tiles (asynchronous double
@@ -1701,8 +1709,11 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const K *__restrict__ kc = A.coord == 0 ? A.ksrc[0] : (A.coord == 1 ? A.ksrc[1] : A.ksrc[2]);
 
-    auto tile_keys = [&](int buf, int d) { return (K *)(dsm + buf * tile_bytes) + (size_t)d * R_TILE; };
-    auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * R_TILE * sizeof(K)); };
+    constexpr uint64_t KMASK = 16 / sizeof(K) - 1, WMASK = 16 / sizeof(WS) - 1;
+    auto tile_keys = [&](int buf, int d) {
+        return (K *)(dsm + buf * tile_bytes + (size_t)d * reorder_key_stride<D, KT>());
+    };
+    auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * reorder_key_stride<D, KT>()); };
     // input index of the item at position e of the level (identity on level 0)
     auto orig = [&](uint64_t e) { return A.isrc ? (uint64_t)A.isrc[e] : e; };
     // carried indices of this thread's items of a tile (loaded one tile ahead)
@@ -1714,28 +1725,39 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
             ix[i] = li < cnt ? (uint32_t)orig(t.ts + li) : 0u;
         }
     };
-    // weight of item li of a tile starting at ts (16-bit weights start at the
-    // even element at or before ts)
-    auto tile_wt = [&](int buf, uint64_t ts) { return tile_w(buf) + (sizeof(WS) == 2 ? (uint32_t)(ts & 1) : 0u); };
+    // the tile's keys and weights (element li at head + li)
+    auto key_head = [&](uint64_t ts) { return (uint32_t)(ts & KMASK); };
+    auto w_head = [&](uint64_t ts) { return A.wsafe ? (uint32_t)(ts & WMASK) : 0u; };
+    auto tile_wt = [&](int buf, uint64_t ts) { return tile_w(buf) + w_head(ts); };
     auto prefetch = [&](const TileRef &t, int buf) {
         const uint32_t cnt = (uint32_t)(t.te - t.ts);
-        if constexpr (sizeof(WS) == 2) {
-            // the 4-byte words covering [ts, te); the last may reach element
-            // te, one past the range: 16-bit weights only ever live in the
-            // engine's 256-byte aligned workspace buffers, where it is readable
-            const uint64_t w0 = t.ts & ~1ull;
-            const uint32_t nw = (uint32_t)((t.te - w0 + 1) >> 1);
-            const uint32_t *src = (const uint32_t *)(A.wsrc + w0);
-            uint32_t *dst = (uint32_t *)tile_w(buf);
-            for (uint32_t q = threadIdx.x; q < nw; q += BLOCK) cp_async<4>(dst + q, src + q);
+        {
+            // keys: the 16-byte chunks covering [ts, te) (engine buffers, 256-byte
+            // aligned, with slack after them, so the chunks stay readable)
+            const uint64_t k0 = t.ts & ~KMASK;
+            const uint32_t nq = (uint32_t)(((t.te - k0) * sizeof(K) + 15) >> 4);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const uint4 *src = (const uint4 *)(A.ksrc[d] + k0);
+                uint4 *dst = (uint4 *)tile_keys(buf, d);
+                for (uint32_t q = threadIdx.x; q < nq; q += BLOCK) cp_async<16>(dst + q, src + q);
+            }
         }
+        if (A.wsafe) {
+            const uint64_t w0 = t.ts & ~WMASK;
+            const uint32_t nq = (uint32_t)(((t.te - w0) * sizeof(WS) + 15) >> 4);
+            const uint4 *src = (const uint4 *)(A.wsrc + w0);
+            uint4 *dst = (uint4 *)tile_w(buf);
+            for (uint32_t q = threadIdx.x; q < nq; q += BLOCK) cp_async<16>(dst + q, src + q);
+        } else if constexpr (sizeof(WS) == 2) {
+            // a caller's 16-bit array does not occur (16-bit weights are the
+            // engine's own copy); kept element-wise for completeness
+            for (uint32_t li = threadIdx.x; li < cnt; li += BLOCK) tile_w(buf)[li] = A.wsrc[t.ts + li];
+        } else {
 #pragma unroll
-        for (int i = 0; i < R_ITEMS; ++i) {
-            const uint32_t li = i * BLOCK + threadIdx.x;
-            if (li < cnt) {
-#pragma unroll
-                for (int d = 0; d < D; ++d) cp_async<sizeof(K)>(tile_keys(buf, d) + li, A.ksrc[d] + t.ts + li);
-                if constexpr (sizeof(WS) != 2) cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
+            for (int i = 0; i < R_ITEMS; ++i) {
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                if (li < cnt) cp_async<sizeof(WS)>(tile_w(buf) + li, A.wsrc + t.ts + li);
             }
         }
         cp_async_commit();
@@ -1879,7 +1901,8 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
                 left_end = p_off + p_nleft;
             }
             const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
-            const K *tkc = tile_keys(buf, A.coord);
+            const uint32_t kh = key_head(cur.ts);
+            const K *tkc = tile_keys(buf, A.coord) + kh;
             const WS *tw = tile_wt(buf, cur.ts);
             uint32_t ix[R_ITEMS];  // carried indices of this thread's items
             if (with_index) {
@@ -1943,19 +1966,22 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
                 }
             }
             __syncthreads();
-            // write the left run and the right run, coalesced
+            // write the left run and the right run, coalesced (both runs are
+            // checked against the segment once per tile)
             const uint64_t left_base = p_off + running;
             const uint64_t right_base = p_off + p_nleft + (cur.ts - p_off - running);
-            for (uint32_t k = threadIdx.x; k < tcount; k += BLOCK) {
+            const bool runs_ok = left_base + tile_left <= left_end && right_base >= left_end &&
+                                 right_base + (tcount - tile_left) <= seg_end;
+            if (!runs_ok && threadIdx.x == 0) atomicOr(&A.rs->err, ERR_SCATTER_BOUNDS);
+            for (uint32_t k = threadIdx.x; runs_ok && k < tcount; k += BLOCK) {
                 const uint32_t src = perm[k];
                 const uint64_t d = k < tile_left ? left_base + k : right_base + (k - tile_left);
-                const bool ok = k < tile_left ? d < left_end : (d >= left_end && d < seg_end);
-                if (!ok || src >= tcount) {
-                    atomicOr(&A.rs->err, ok ? ERR_TILE_PERM : ERR_SCATTER_BOUNDS);
+                if (src >= tcount) {
+                    atomicOr(&A.rs->err, ERR_TILE_PERM);
                     continue;
                 }
 #pragma unroll
-                for (int dd = 0; dd < D; ++dd) A.kdst[dd][d] = tile_keys(buf, dd)[src];
+                for (int dd = 0; dd < D; ++dd) A.kdst[dd][d] = tile_keys(buf, dd)[kh + src];
                 A.wdst[d] = tw[src];
                 if (with_index) A.idst[d] = s_idx[src];
             }

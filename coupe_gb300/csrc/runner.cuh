@@ -374,6 +374,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             R.kdst[d] = B.keys[kb_next][d];
         }
         R.wsrc = wc;
+        R.wsafe = level0 && w_in == (const WS *)a.d_weights ? 0 : 1;  // the caller's array: element copies
         R.wdst = (WS *)B.w[snext];
         R.isrc = ic;
         R.idst = carry ? B.idx[snext] : nullptr;
@@ -514,7 +515,9 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     const bool carry = index_path || KT::BAND;
     const uint64_t nsets = multi ? a.nsets : 0;
     const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
-    int rc = ensure_workspace(C, need, err);
+    // 256 bytes of slack: reorder tiles are copied in 16-byte chunks that may
+    // end up to 15 bytes past a buffer
+    int rc = ensure_workspace(C, need + 256, err);
     if (rc != COUPE_ERR_OK) return rc;
     Bump real{(char *)C.ws, 0};
     B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
