@@ -250,13 +250,17 @@ def main():
         ids_by_mode[mode] = part.cpu().numpy().view(np.uint64).copy()
     stats = coupe.last_stats()
 
-    # live roofline: per-kernel CUDA-event times over K more steps
-    coupe.profile(True)
-    for _ in range(args.steps):
-        coupe.rcb_device(part, pts, w, iters, tol, mode=headline)
-    torch.cuda.synchronize()
-    prof = coupe.profile_read()
-    coupe.profile(False)
+    # live roofline: per-kernel CUDA-event times over K more steps (every
+    # mode, for the per-kernel comparison; the headline mode's for the roofline)
+    by_mode = {}
+    for mode in modes:
+        coupe.profile(True)
+        for _ in range(args.steps):
+            coupe.rcb_device(part, pts, w, iters, tol, mode=mode)
+        torch.cuda.synchronize()
+        by_mode[mode] = coupe.profile_read()
+        coupe.profile(False)
+    prof = by_mode[headline]
     total_ms = sum(v["ms"] for v in prof.values()) or 1.0
     top = max(prof.items(), key=lambda kv: kv[1]["ms"])
     peak, peak_kind = measured_peak()
@@ -320,7 +324,9 @@ def main():
         "roofline": roofline,
         "run": {"splits": stats["splits"], "split_steps": stats["split_steps"],
                 "max_split_steps": stats["max_split_steps"], "hist_passes": stats["hist_passes"],
-                "algo_bytes": stats["algo_bytes"], "kernel_launches_per_step": stats["kernel_launches"]},
+                "algo_bytes": stats["algo_bytes"], "kernel_launches_per_step": stats["kernel_launches"],
+                "kernel_us_per_step": {m: {k: round(1e3 * v["ms"] / args.steps, 1) for k, v in pr.items()}
+                                       for m, pr in by_mode.items()}},
         "parity": parity,
         "clocks": clocks.summary() if clocks else None,
     }

@@ -819,8 +819,6 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         }
         __syncthreads();
         const BinGuess g = bin_guess<KT>(lo, hi, NB);
-        // band form: bounds of the interval's ends (f64 work: once per piece)
-        CutBounds blo = {0.f, 0.f}, bhi = {0.f, 0.f};
         bool xpend = false;  // band form: a decision waits for an exact minimum
         uint32_t xkey = 0;
         uint64_t xcut = 0;
@@ -828,8 +826,6 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         uint32_t nband = 0;   // band form: f64 coordinates this thread read
         uint32_t qn = 0;      // band form: entries in this warp's queue (same in every lane)
         if constexpr (KT::BAND) {
-            blo = band_bounds(lo);
-            bhi = band_bounds(hi);
             xpend = sg.xstate == X_PENDING;
             xkey = sg.xkey;
             xcut = sg.xcut;
@@ -881,14 +877,16 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             }
         };
         for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HIST_ITEMS) {
+            // items of this iteration: 32-bit offsets from base below lim
+            const uint32_t lim = (uint32_t)min((uint64_t)BLOCK * HIST_ITEMS, b - base);
             K kv[HIST_ITEMS];
             typename WT::S wv[HIST_ITEMS];
 #pragma unroll
             for (int i = 0; i < HIST_ITEMS; ++i) {
-                const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
-                if (e < b) {
-                    kv[i] = keys[e];
-                    wv[i] = wts[e];
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                if (li < lim) {
+                    kv[i] = keys[base + li];
+                    wv[i] = wts[base + li];
                 }
             }
             if constexpr (KT::BAND) {
@@ -900,20 +898,21 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                 uint32_t slow = 0;
 #pragma unroll
                 for (int i = 0; i < HIST_ITEMS; ++i) {
-                    const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
-                    if (L > 1 && accx && e < b && KT::isnan(kv[i])) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    if (L > 1 && accx && li < lim && KT::isnan(kv[i])) {
                         uint64_t q[L];
                         item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
                     }
-                    if (e < b && !KT::isnan(kv[i])) {
+                    if (li < lim && !KT::isnan(kv[i])) {
                         if (xpend && KT::ord(kv[i]) == xkey) {
                             slow |= 1u << i;
                             continue;
                         }
-                        const int sl = band_side(kv[i], blo), sh = band_side(kv[i], bhi);
-                        bool in_band = sl == 0 || (sl > 0 && sh == 0);
-                        int bin = 0;
-                        if (sl > 0 && sh < 0) bin = bin_band<KT>(kv[i], cuts, cb_lo, cb_hi, NB, g, in_band);
+                        // keys outside the interval land in the edge bins like
+                        // their neighbours inside it; edge-bin sums stay in
+                        // registers (most keys once the interval has narrowed)
+                        bool in_band;
+                        const int bin = bin_band<KT>(kv[i], cuts, cb_lo, cb_hi, NB, g, in_band);
                         if (in_band) {
                             slow |= 1u << i;
                             continue;
@@ -921,9 +920,9 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                         uint64_t q[L];
                         item_q(wv[i], q);
                         const O v = (O)~KT::ord(kv[i]);
-                        if (sl < 0 || sh > 0) {
+                        if (bin == 0 || bin == NB - 1) {
                             // constant indices only: keeps the sums in registers
-                            if (sl < 0) {
+                            if (bin == 0) {
                                 out_c[0] += 1;
 #pragma unroll
                                 for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
@@ -954,7 +953,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                         const uint32_t m = __ballot_sync(0xffffffffu, bit);
                         if (bit)
                             s_q[warp][qn + __popc(m & ((1u << lane) - 1))] =
-                                (uint32_t)(base + (uint64_t)i * BLOCK + threadIdx.x - a);
+                                (uint32_t)(base - a) + i * BLOCK + threadIdx.x;
                         qn += __popc(m);
                         if (qn >= 32) {
                             __syncwarp();
@@ -972,12 +971,12 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             } else {
 #pragma unroll
             for (int i = 0; i < HIST_ITEMS; ++i) {
-                const uint64_t e = base + (uint64_t)i * BLOCK + threadIdx.x;
-                if (L > 1 && accx && e < b && KT::isnan(kv[i])) {
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                if (L > 1 && accx && li < lim && KT::isnan(kv[i])) {
                     uint64_t q[L];
                     item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
                 }
-                if (e < b && !KT::isnan(kv[i])) {
+                if (li < lim && !KT::isnan(kv[i])) {
                     uint64_t q[L];
                     item_q(wv[i], q);
                     const bool below = KT::lt(kv[i], lo), above = !below && !KT::lt(kv[i], hi);
@@ -1280,9 +1279,10 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         // interval of weight_left values that contains sum/2 (f64 rounding is
         // monotone), so two ends that agree settle it, unless both fail on
         // either side of sum/2; `hi <= t + dist` is monotone in dist.
+        // (f64 division is slow here: the upper end only with truncated bins)
         const bool p_lo = fabs((WT::f64(wl) - ideal) / ideal) <= tol;
-        const bool p_hi = fabs((WT::f64(wl_hi) - ideal) / ideal) <= tol;
-        const bool spans = ideal != 0.0 && WT::f64(wl) <= ideal && ideal <= WT::f64(wl_hi);
+        const bool p_hi = apx ? fabs((WT::f64(wl_hi) - ideal) / ideal) <= tol : p_lo;
+        const bool spans = apx && ideal != 0.0 && WT::f64(wl) <= ideal && ideal <= WT::f64(wl_hi);
         const bool imb_yes = p_lo && p_hi, imb_no = !p_lo && !p_hi && !(spans && tol >= 0.0);
         const bool near_lo = hv <= tv + dl, near_hi = hv <= tv + dh;
         const bool stop = count == prev || near_lo || imb_yes;
@@ -1291,7 +1291,7 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             need_x = near_hi;  // band form: only the exact minimum tells
             need_w = !imb_no;
             // coupe's update (:564-571) is monotone in weight_left
-            if (!need_x && !need_w && WT::less(wl, WT::sub(sum, wl)) != WT::less(wl_hi, WT::sub(sum, wl_hi)))
+            if (apx && !need_x && !need_w && WT::less(wl, WT::sub(sum, wl)) != WT::less(wl_hi, WT::sub(sum, wl_hi)))
                 need_w = true;
         }
         if (need_x || need_w) {
