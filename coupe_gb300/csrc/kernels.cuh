@@ -74,6 +74,28 @@ __device__ __forceinline__ uint64_t warp_min_ord<uint64_t>(uint64_t v) {
 
 // Exclusive scan of one u64 per thread over the block; returns the prefix
 // and writes the block total.  `sh` holds NWARPS + 1 words.
+// Inclusive prefix sum over the lanes of a warp.
+__device__ __forceinline__ uint64_t warp_incl_scan_u64(uint64_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= o) v += u;
+    }
+    return v;
+}
+// Minimum over lanes [lane, 31] of a warp.
+template <class O>
+__device__ __forceinline__ O warp_suffix_min(O v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const O u = __shfl_down_sync(0xffffffffu, v, o);
+        if (lane + o < 32 && u < v) v = u;
+    }
+    return v;
+}
+
 __device__ __forceinline__ uint64_t block_exscan_u64(uint64_t v, uint64_t *sh, uint64_t &total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint64_t inc = v;
@@ -1130,7 +1152,22 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 #pragma unroll
     for (int l = 0; l < L; ++l) Tw[l] = 0;
     if (lane * BS < NB) {
-        for (int j = 0; j < BS; ++j) {
+        // four bins per step, their loads in flight together
+        int j = 0;
+        for (; j + 4 <= BS; j += 4) {
+            uint64_t c[4], w[4][L];
+            O m[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) load_bin(lane * BS + j + i, c[i], w[i], m[i]);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                Tc += c[i];
+#pragma unroll
+                for (int l = 0; l < L; ++l) Tw[l] += w[i][l];
+                Tm = m[i] < Tm ? m[i] : Tm;
+            }
+        }
+        for (; j < BS; ++j) {
             uint64_t c, w[L];
             O m;
             load_bin(lane * BS + j, c, w, m);
@@ -1140,10 +1177,18 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             Tm = m < Tm ? m : Tm;
         }
     }
+    // Each step needs only the bins below the cut (count and weight left:
+    // a prefix sum) and the smallest key at or above it (a suffix minimum),
+    // so both are scanned once over the lane blocks and each step reads them
+    // with one shuffle.
+    uint64_t Ic = warp_incl_scan_u64(Tc), Iw[L];
+#pragma unroll
+    for (int l = 0; l < L; ++l) Iw[l] = warp_incl_scan_u64(Tw[l]);
+    const O Sm = warp_suffix_min<O>(Tm);
     // Every binned key belongs to this segment.  More counts than items means
     // corrupt bins: no split is taken from them (the host stops the run before
     // any later kernel could use sizes derived from them).
-    if (warp_sum_u64(Tc) > sg.n) {
+    if (__shfl_sync(0xffffffffu, Ic, 31) > sg.n) {
         if (lane == 0) {
             flags[k] = 0;
             if (atomicOr(&rs->err, ERR_COUNT_MISMATCH) == 0) {
@@ -1153,12 +1198,15 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         }
         return;
     }
+    // Once half of the interval is narrower than a block, the one block left
+    // (fine_base ...) is spread over the lanes, one bin each, and scanned the
+    // same way, on top of the prefix below the block and the minimum above it.
     bool fine = false;
     int fine_base = 0;
-    uint64_t Fc = 0, Fw[L];
-    O Fm = NONE;
+    uint64_t IFc = 0, IFw[L], Bc = 0, Bw[L];
+    O FSm = NONE, Am = NONE;
 #pragma unroll
-    for (int l = 0; l < L; ++l) Fw[l] = 0;
+    for (int l = 0; l < L; ++l) IFw[l] = Bw[l] = 0;
 
     // the level's first decisions settle a child's sum from exact sums of
     // the first pass: coupe's weight_left for a left child, sum - weight_left
@@ -1173,11 +1221,6 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     K lo = sg.lo, hi = sg.hi;
     uint64_t prev = sg.prev;
     int lo_b = 0, hi_b = NB;
-    uint64_t cnt_below = 0;
-    uint64_t w_below[L];
-#pragma unroll
-    for (int l = 0; l < L; ++l) w_below[l] = 0;
-    O kmin_above = NONE;
     bool flag_exact = false;  // band form: a test needs an exact minimum first
     bool flag_exactw = false;  // f64 weights: a test needs exact bins first
     K xcut = 0;
@@ -1193,30 +1236,53 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         if (!fine && mid_b - lo_b < BS) {
             fine = true;
             fine_base = lo_b - lo_b % BS;  // the block holding [lo_b, hi_b)
-            if (lane < BS) load_bin(fine_base + lane, Fc, Fw, Fm);
+            const int f = fine_base / BS;
+            uint64_t c = 0, w[L];
+            O m = NONE;
+#pragma unroll
+            for (int l = 0; l < L; ++l) w[l] = 0;
+            if (lane < BS) load_bin(fine_base + lane, c, w, m);
+            IFc = warp_incl_scan_u64(c);
+#pragma unroll
+            for (int l = 0; l < L; ++l) IFw[l] = warp_incl_scan_u64(w[l]);
+            FSm = warp_suffix_min<O>(m);
+            // prefix below block f, minimum above it
+            const uint64_t pc = __shfl_sync(0xffffffffu, Ic, f > 0 ? f - 1 : 0);
+            Bc = f > 0 ? pc : 0;
+#pragma unroll
+            for (int l = 0; l < L; ++l) {
+                const uint64_t pw = __shfl_sync(0xffffffffu, Iw[l], f > 0 ? f - 1 : 0);
+                Bw[l] = f > 0 ? pw : 0;
+            }
+            const O am = __shfl_sync(0xffffffffu, Sm, f + 1 < 32 ? f + 1 : 31);
+            Am = f + 1 < 32 ? am : NONE;
         }
-        // this lane's unit: a whole block (coarse) or one bin (fine)
-        const int u0 = fine ? fine_base + lane : lane * BS;
-        const bool has = fine ? lane < BS : u0 < NB;
-        uint64_t c = 0, wp[L];
-        O m = NONE;
+        // count and weight of the bins below mid_b, smallest key at or above it
+        uint64_t count, wacc[L];
+        O kminO;
+        if (!fine) {
+            const int ml = mid_b / BS;  // a block boundary
+            const uint64_t pc = __shfl_sync(0xffffffffu, Ic, ml > 0 ? ml - 1 : 0);
+            count = ml > 0 ? pc : 0;
 #pragma unroll
-        for (int l = 0; l < L; ++l) wp[l] = 0;
-        if (has && u0 >= lo_b && u0 < mid_b) {
-            c = fine ? Fc : Tc;
+            for (int l = 0; l < L; ++l) {
+                const uint64_t pw = __shfl_sync(0xffffffffu, Iw[l], ml > 0 ? ml - 1 : 0);
+                wacc[l] = ml > 0 ? pw : 0;
+            }
+            const O sm = __shfl_sync(0xffffffffu, Sm, ml < 32 ? ml : 31);
+            kminO = ml < 32 ? sm : NONE;
+        } else {
+            const int j = mid_b - fine_base;  // < BS
+            const uint64_t pc = __shfl_sync(0xffffffffu, IFc, j > 0 ? j - 1 : 0);
+            count = Bc + (j > 0 ? pc : 0);
 #pragma unroll
-            for (int l = 0; l < L; ++l) wp[l] = fine ? Fw[l] : Tw[l];
+            for (int l = 0; l < L; ++l) {
+                const uint64_t pw = __shfl_sync(0xffffffffu, IFw[l], j > 0 ? j - 1 : 0);
+                wacc[l] = Bw[l] + (j > 0 ? pw : 0);
+            }
+            const O sm = __shfl_sync(0xffffffffu, FSm, j);
+            kminO = sm < Am ? sm : Am;
         }
-        if (has && u0 >= mid_b && u0 < hi_b) m = fine ? Fm : Tm;
-        c = warp_sum_u64(c);
-#pragma unroll
-        for (int l = 0; l < L; ++l) wp[l] = warp_sum_u64(wp[l]);
-        m = warp_min_ord<O>(m);
-        const uint64_t count = cnt_below + c;
-        uint64_t wacc[L];
-#pragma unroll
-        for (int l = 0; l < L; ++l) wacc[l] = w_below[l] + wp[l];
-        const O kminO = m < kmin_above ? m : kmin_above;
         const K t = KT::cmid(lo, hi);
         const typename KT::A tv = KT::cval(t), hv = KT::cval(hi);
         // distance of the nearest item on the right (recursive_bisection.rs:487):
@@ -1253,7 +1319,6 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
             hi = t;
             prev = count;
             hi_b = mid_b;
-            kmin_above = kminO;
             continue;
         }
         if (flag_exact) {
@@ -1327,13 +1392,9 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         if (WT::less(wl, WT::sub(sum, wl))) {
             lo = t;
             lo_b = mid_b;
-            cnt_below = count;
-#pragma unroll
-            for (int l = 0; l < L; ++l) w_below[l] = wacc[l];
         } else {
             hi = t;
             hi_b = mid_b;
-            kmin_above = kminO;
         }
     }
     const uint32_t total_steps = sg.steps + steps;
