@@ -503,7 +503,7 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
     const int reps = repeats < 1 ? 1 : (repeats > 15 ? 15 : repeats);
     double best_ms = 1e300;
     cg::Tuning best_t = keep;
-    for (int nbk : {10, 9, 8})
+    for (int nbk : {10, 9, 8, 7, 6})
         for (int hc : {0, 3, 2})
             for (int rc : {1, 2}) {
                 t = keep;

@@ -615,7 +615,7 @@ static __global__ void k_sets_init(SetTab sets) {
 // !(key < c), i.e. the leaf reached by descending the tree with
 // `key < c ? left : right`; bins are in key order.
 // ---------------------------------------------------------------------------
-template <class KT>
+template <class KT, bool WARP = false>
 __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT::C hi, int nbk,
                                                   typename KT::C *cuts, float *cb_lo = nullptr,
                                                   float *cb_hi = nullptr) {
@@ -625,11 +625,12 @@ __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT
     // r - h and r + h (or lo / hi beyond the ends), which are exactly the
     // ancestors coupe's loop would have reached it from; one midpoint per cut
     // (f64 midpoints are costly on GB300).  Contains barriers: every thread of
-    // the block calls it.
+    // the block (or with WARP, of the warp) calls it.
     const int nb = 1 << nbk;
+    const int tr = WARP ? (threadIdx.x & 31) : threadIdx.x, TS = WARP ? 32 : blockDim.x;
     for (int d = 0; d < nbk; ++d) {
         const int h = 1 << (nbk - 1 - d);
-        for (int p = threadIdx.x; p < (1 << d); p += blockDim.x) {
+        for (int p = tr; p < (1 << d); p += TS) {
             const int r = (2 * p + 1) * h - 1;
             const K a = r - h < 0 ? lo : cuts[r - h];
             const K b = r + h >= nb - 1 ? hi : cuts[r + h];
@@ -641,7 +642,10 @@ __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT
                 cb_hi[r] = cb.hi;
             }
         }
-        __syncthreads();
+        if (WARP)
+            __syncwarp();
+        else
+            __syncthreads();
     }
 }
 
@@ -784,7 +788,153 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     uint32_t k = upper_index(P, nlist + 1, c0);
     uint64_t pos = c0;
     int cur_s = -1;
+    // Small segments (at most SMALL_SEG items, at most SNB bins), whole in
+    // this CTA's range, are binned one per warp, up to NWARPS at once, each
+    // warp on its own slice of the shared arrays with warp barriers only
+    // (the CTA path below costs a dozen block barriers per piece).  One item
+    // per lane per step; a band item's f64 coordinate is read in place.
+    constexpr int SNB = HNB / NWARPS;
+    constexpr uint64_t SMALL_SEG = 4096;
+    auto small_seg = [&](const uint32_t kk) {
+        const uint32_t s = list[kk];
+        const Seg<KT> &sg = segs[s];
+        const int sfs = L > 1 ? (set_fs ? set_fs[sg.set] : rs->fscale) : 0;
+        const int sqb = L > 1 && set_fs ? set_qb[sg.set] : (L > 1 ? rs->qb : 0);
+        const bool apx = fapprox && sg.exactw == 0;
+        const bool spk = packed_all || apx;
+        const bool accx = L > 1 && sg.sumx != SUMX_NONE;
+        CK *const wc = cuts + warp * SNB;
+        float *const wlo = cb_lo + (KT::BAND ? warp * SNB : 0), *const whi = cb_hi + (KT::BAND ? warp * SNB : 0);
+        uint64_t *const wsw = sw + warp * SNB * L;
+        uint32_t *const wcnt = scnt + warp * SNB;
+        O *const winv = sinv + warp * SNB;
+        const CK lo = sg.lo, hi = sg.hi;
+        build_sorted_cuts<KT, true>(lo, hi, nbk, wc, wlo, whi);
+        for (int i = lane; i < NB; i += 32) {
+            wcnt[i] = 0;
+            winv[i] = 0;
+#pragma unroll
+            for (int l = 0; l < L; ++l) wsw[i * L + l] = 0;
+        }
+        __syncwarp();
+        const BinGuess g = bin_guess<KT>(lo, hi, NB);
+        uint64_t xacc[L];
+#pragma unroll
+        for (int l = 0; l < L; ++l) xacc[l] = 0;
+        uint64_t xm = ~0ull;
+        uint32_t nband = 0;
+        const uint64_t a = sg.off, b = a + P[kk + 1] - P[kk];
+        for (uint64_t e = a + lane; e < b; e += 32) {
+            const K kv = keys[e];
+            uint64_t q[L];
+            if constexpr (L > 1) {
+                const unsigned __int128 qq = fixed_q_bits((double)wts[e], sfs);
+                if (accx) {
+                    xacc[0] += (uint32_t)qq;
+                    xacc[1] += (uint32_t)(qq >> 32);
+                    xacc[2] += (uint32_t)(qq >> 64);
+                    xacc[3] += (uint32_t)(qq >> 96);
+                }
+                if (apx) {
+                    q[0] = (uint64_t)(qq >> sqb);
+#pragma unroll
+                    for (int l = 1; l < L; ++l) q[l] = 0;
+                } else {
+                    q[0] = (uint32_t)qq;
+                    q[1] = (uint32_t)(qq >> 32);
+                    q[2] = (uint32_t)(qq >> 64);
+                    q[3] = (uint32_t)(qq >> 96);
+                }
+            } else {
+                WT::limbs(wts[e], sfs, q);
+            }
+            if (KT::isnan(kv)) continue;  // not binned; its weight is in the sum
+            int bin;
+            if constexpr (KT::BAND) {
+                bool in_band;
+                bin = bin_band<KT>(kv, wc, wlo, whi, NB, g, in_band);
+                const bool pend = sg.xstate == X_PENDING && KT::ord(kv) == sg.xkey;
+                if (in_band || pend) {
+                    // the key's bin is a lower bound; the f64 coordinate decides
+                    const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
+                    ++nband;
+                    if (pend && !KeyF64::lt(c, sg.xcut)) xm = c < xm ? c : xm;
+                    bin = bin_band_exact(bin, c, wc, NB);
+                }
+            } else {
+                bin = bin_sorted<KT>(kv, wc, NB, g);
+            }
+            if (spk) {
+                atomicAdd((unsigned long long *)&wsw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+            } else {
+                atomicAdd(&wcnt[bin], 1u);
+#pragma unroll
+                for (int l = 0; l < L; ++l)
+                    if (q[l]) atomicAdd((unsigned long long *)&wsw[bin * L + l], (unsigned long long)q[l]);
+            }
+            const O v = (O)~KT::ord(kv);
+            if (v > winv[bin]) atomic_max_ord(&winv[bin], v);
+        }
+        if constexpr (L > 1) {
+            if (accx) {
+#pragma unroll
+                for (int l = 0; l < L; ++l) {
+                    const uint64_t v = warp_sum_u64(xacc[l]);
+                    if (lane == 0 && v) atomicAdd((unsigned long long *)&segs_w[s].xq[l], (unsigned long long)v);
+                }
+            }
+        }
+        if constexpr (KT::BAND) {
+            const uint64_t xw = warp_min_u64(xm);
+            const uint64_t nw = warp_sum_u64(nband);
+            if (lane == 0) {
+                if (xw != ~0ull) atomicMin((unsigned long long *)&segs_w[s].xmin, (unsigned long long)xw);
+                if (nw) atomicAdd(bs.count, (unsigned long long)nw);
+            }
+        }
+        __syncwarp();
+        for (int i = lane; i < NB; i += 32) {
+            uint32_t c;
+            uint64_t wl[L];
+            if (spk) {
+                c = (uint32_t)(wsw[i] >> PACK_SHIFT);
+                wl[0] = wsw[i] & PACK_WMASK;
+#pragma unroll
+                for (int l = 1; l < L; ++l) wl[l] = 0;
+            } else {
+                c = wcnt[i];
+#pragma unroll
+                for (int l = 0; l < L; ++l) wl[l] = wsw[i * L + l];
+            }
+            if (c) {
+                const size_t gi = (size_t)s * NB + i;
+                atomicAdd(&H.cnt[gi], c);
+#pragma unroll
+                for (int l = 0; l < L; ++l)
+                    if (wl[l]) atomicAdd((unsigned long long *)&H.w[gi * L + l], (unsigned long long)wl[l]);
+                atomic_max_ord(&H.inv[gi], winv[i]);
+            }
+        }
+    };
     while (pos < c1) {
+        // whole small segments from pos on: one per warp
+        uint32_t m = 0;
+        if (NB <= SNB) {
+            while (m < NWARPS && k + m < nlist) {
+                const uint64_t p0 = P[k + m], p1 = P[k + m + 1];
+                if ((m == 0 && p0 != pos) || p1 > c1 || p1 - p0 > SMALL_SEG) break;
+                ++m;
+            }
+        }
+        if (m > 0) {
+            __syncthreads();  // the shared arrays' previous users are done
+            if (warp < (int)m) small_seg(k + warp);
+            __syncthreads();
+            pos = P[k + m];
+            k += m;
+            cur_s = -1;
+            continue;
+        }
         const uint32_t s = list[k];
         const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
         const Seg<KT> &sg = segs[s];

@@ -195,8 +195,9 @@ struct coupe_gpu_tuning {
  * candidate schedule of the knobs above, `repeats` timed runs each after one
  * warm-up, and keeps the fastest process-wide (the ids are the same under
  * every schedule).  `best` (may be NULL) receives the choice; d_partition
- * holds the ids of the last run.  18 candidates: budget about
- * 18 * (repeats + 1) runs of the workload. */
+ * holds the ids of the last run.  30 candidates (bisection steps per pass
+ * 6-10, histogram CTAs per SM 0/3/2, reorder chunks per CTA 1/2): budget
+ * about 30 * (repeats + 1) runs of the workload. */
 enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets,
 		const uint64_t *set_offsets, uint64_t dimension, const double *d_points,
 		enum coupe_type weight_type, const void *d_weights,

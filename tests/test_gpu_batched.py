@@ -147,7 +147,7 @@ def test_autotune_keeps_ids(coupe, oracle_mod):
         dw = torch.from_numpy(w).cuda()
         ids = torch.zeros(len(pts), dtype=torch.int64, device="cuda")
         best = coupe.autotune_device(ids, dp, dw, off, it, 0.01, mode="f32key_f64band", repeats=1)
-        assert best["max_nbk"] in (8, 9, 10) and best["hist_ctas_per_sm"] in (0, 2, 3)
+        assert best["max_nbk"] in (6, 7, 8, 9, 10) and best["hist_ctas_per_sm"] in (0, 2, 3)
         assert best["reorder_chunks_per_cta"] in (1, 2) and best["device_ms"] > 0
         assert {k: coupe.get_option(k) for k in names} == {k: best[k] for k in names}
         assert np.array_equal(ids.cpu().numpy().astype(np.uint64), want)

@@ -442,3 +442,27 @@ def test_f64_weights_negative_use_exact_bins(coupe, oracle_mod):
         got = _gpu(coupe, pts, w, 7, 0.01, mode=mode)
         assert coupe.last_stats()["weight_rechecks"] == 0
         assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f64", "f32key_f64band"])
+@pytest.mark.parametrize("nbk,exact", [(6, 0), (7, 1), (4, 0)])
+def test_small_segments_binned_per_warp(coupe, oracle_mod, mode, nbk, exact):
+    """With at most 128 bins a pass, segments of up to 4096 items are binned
+    one per warp: ids equal the oracle's, for int64 and f64 weights, NaN keys
+    and keys piled on a few values (band items)."""
+    rng = np.random.default_rng(90 + nbk)
+    n = 150_000
+    pts = rng.random((n, 3))
+    pts[::7, 0] = 0.5
+    pts[::11, 1] = np.round(pts[::11, 1], 2)
+    pts[5::997, 2] = np.nan
+    try:
+        coupe.set_option("max_nbk", nbk)
+        coupe.set_option("exact_f64_hist", exact)
+        for w in (rng.integers(1, 50, n, dtype=np.int64), rng.lognormal(0.0, 1.0, n)):
+            want, _ = oracle_mod.rcb(pts, w, 11, 0.01, mode=_oracle_mode(mode) | oracle_mod.NAN_RIGHT)
+            got = _gpu(coupe, pts, w, 11, 0.01, mode=mode)
+            assert np.array_equal(got, want)
+    finally:
+        coupe.set_option("max_nbk", 10)
+        coupe.set_option("exact_f64_hist", 0)
