@@ -555,6 +555,8 @@ struct RunScalars {
     int32_t qb;                      // f64 weights, one set: shift of the approximate binned weights
     uint32_t fapprox;                // f64 weights: bins hold approximate weights (see k_hist)
     uint32_t nexactw;                // decisions that needed exact f64 weight sums
+    uint32_t decide_done;            // CTAs of the running k_decide that finished (reset by the last)
+    uint32_t pad3;
 };
 
 }  // namespace cg

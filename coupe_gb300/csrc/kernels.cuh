@@ -1257,16 +1257,46 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     }
 }
 
+// Compacts the listed segments still searching into list2 with the exclusive
+// prefix P2 of their sizes.  One CTA.
+template <class KT>
+__device__ __forceinline__ void scan_list_block(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+                                                const uint32_t *__restrict__ flags, uint32_t nlist, uint32_t *list2,
+                                                uint64_t *P2, RunScalars *rs) {
+    __shared__ uint64_t sh[33];
+    uint64_t outc = 0, run = 0;
+    for (uint32_t base = 0; base < nlist; base += blockDim.x) {
+        const uint32_t k = base + threadIdx.x;
+        const bool keep = k < nlist && flags[k];
+        const uint32_t s = keep ? list[k] : 0;
+        const uint64_t sz = keep ? segs[s].n : 0;
+        uint64_t tc, tp;
+        const uint64_t ci = block_exscan_u64(keep ? 1 : 0, sh, tc);
+        const uint64_t pi = block_exscan_u64(sz, sh, tp);
+        if (keep) {
+            list2[outc + ci] = s;
+            P2[outc + ci] = run + pi;
+        }
+        outc += tc;
+        run += tp;
+    }
+    if (threadIdx.x == 0) {
+        P2[outc] = run;
+        rs->nactive = outc;
+        rs->total_active = run;
+        rs->pass_points += run;  // read by the pass that follows
+    }
+}
+
 // ---------------------------------------------------------------------------
 // k_decide: replays coupe's split loop (recursive_bisection.rs:470-572) for
 // up to nbk steps per segment from its bins.  One warp per listed segment;
 // every lane computes the same decisions.
 // ---------------------------------------------------------------------------
 template <class KT, class WT>
-__global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
-                                                  Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
-                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs,
-                                                  const int32_t *__restrict__ set_qb) {
+__device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__restrict__ list, const uint32_t k,
+                                           Hist<KT, WT> H, int nbk, double tol, uint32_t *flags, RunScalars *rs,
+                                           const int32_t *__restrict__ set_fs, const int32_t *__restrict__ set_qb) {
     typedef typename KT::C K;  // cuts and interval bounds
     typedef typename KT::Ord O;
     typedef typename WT::V V;
@@ -1274,9 +1304,6 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     // band form: empty bins hold no key at all (not +inf, a possible key)
     constexpr O NONE = KT::BAND ? (O)~(O)0 : KT::ORD_INF;
     const int lane = threadIdx.x & 31;
-    const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
-    if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass (the grid is an upper bound)
-    if (k >= nlist) return;
     const uint32_t s = list[k];
     Seg<KT> sg = segs[s];
     const int NB = 1 << nbk;
@@ -1608,44 +1635,31 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     }
 }
 
-// Compacts the listed segments still searching into list2 with the exclusive
-// prefix P2 of their sizes.  One CTA.
-template <class KT>
-__global__ void __launch_bounds__(1024) k_scan_list(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
-                                                    const uint32_t *__restrict__ flags, uint32_t nlist,
-                                                    uint32_t *list2, uint64_t *P2, RunScalars *rs, int nlist_dev) {
-    __shared__ uint64_t sh[33];
-    __shared__ uint32_t s_nlist;
-    if (nlist_dev) {
-        // a speculative pass: its list is the one the last scan left; read it
-        // before thread 0 overwrites the count below
-        if (threadIdx.x == 0) s_nlist = (uint32_t)rs->nactive;
-        __syncthreads();
-        nlist = s_nlist;
-    }
-    uint64_t outc = 0, run = 0;
-    for (uint32_t base = 0; base < nlist; base += blockDim.x) {
-        const uint32_t k = base + threadIdx.x;
-        const bool keep = k < nlist && flags[k];
-        const uint32_t s = keep ? list[k] : 0;
-        const uint64_t sz = keep ? segs[s].n : 0;
-        uint64_t tc, tp;
-        const uint64_t ci = block_exscan_u64(keep ? 1 : 0, sh, tc);
-        const uint64_t pi = block_exscan_u64(sz, sh, tp);
-        if (keep) {
-            list2[outc + ci] = s;
-            P2[outc + ci] = run + pi;
-        }
-        outc += tc;
-        run += tp;
-    }
-    if (threadIdx.x == 0) {
-        P2[outc] = run;
-        rs->nactive = outc;
-        rs->total_active = run;
-        rs->pass_points += run;  // read by the pass that follows
+// One warp per listed segment (decide_one); then the last CTA to finish lists
+// the segments still searching and the prefix of their sizes for the next
+// pass (list2, P2, rs->nactive).
+template <class KT, class WT>
+__global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
+                                                  Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
+                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs,
+                                                  const int32_t *__restrict__ set_qb, uint32_t *list2, uint64_t *P2) {
+    __shared__ uint32_t s_last;
+    // a speculative pass: the list the last scan left (the grid is an upper
+    // bound); every CTA reads it before the last one overwrites it
+    if (nlist_dev) nlist = (uint32_t)rs->nactive;
+    const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
+    if (k < nlist) decide_one<KT, WT>(segs, list, k, H, nbk, tol, flags, rs, set_fs, set_qb);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&rs->decide_done, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (s_last) {
+        __threadfence();
+        scan_list_block<KT>(segs, list, flags, nlist, list2, P2, rs);
+        if (threadIdx.x == 0) rs->decide_done = 0;
     }
 }
+
 
 // Builds the next level's segments from the finished splits: left child
 // (heap 2h+1, sum = weight_left, bbox max[coord] = split_pos) and right child

@@ -254,9 +254,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         bytes += V * (sk + sw);
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
-                                                                 B.flags, B.rs, 0, set_fs, set_qb));
-        CG_LAUNCH(KID_SCAN, 0,
-                  k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[0], B.flags, (uint32_t)S, B.list[1], B.P[1], B.rs, 0));
+                                                                 B.flags, B.rs, 0, set_fs, set_qb, B.list[1], B.P[1]));
         // A speculative second pass over list[1] without asking the host how
         // long it is: its kernels read the count the scan left and return at
         // once when no segment is searching.  The next scan leaves list[0].
@@ -266,9 +264,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         ++st->hist_passes;
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
-                                                                 B.rs, 1, set_fs, set_qb));
-        CG_LAUNCH(KID_SCAN, 0,
-                  k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[1], B.flags, 0, B.list[0], B.P[0], B.rs, 1));
+                                                                 B.rs, 1, set_fs, set_qb, B.list[0], B.P[0]));
         // k_children returns at once if a segment is still searching
         if (!last) {
             const int rc_ = children();
@@ -297,10 +293,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             ++st->hist_passes;
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
-                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs, set_qb));
-            CG_LAUNCH(KID_SCAN, 0,
-                      k_scan_list<KT><<<1, 1024, 0, s>>>(segs, B.list[li], B.flags, (uint32_t)nlist, B.list[li ^ 1],
-                                                         B.P[li ^ 1], B.rs, 0));
+                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs, set_qb,
+                          B.list[li ^ 1], B.P[li ^ 1]));
             li ^= 1;
             CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
             CG_CK(cudaStreamSynchronize(s));
