@@ -1257,6 +1257,204 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     }
 }
 
+// Builds the next level's segments from the finished splits: left child
+// (heap 2h+1, sum = weight_left, bbox max[coord] = split_pos) and right child
+// (2h+2, sum - weight_left, bbox min[coord] = split_pos), empty children
+// dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
+// the smallest heap id among the children (the id offset, :698-702).
+enum : int { CHILD_ALL = 0, CHILD_COUNT = 1, CHILD_SCAN = 2, CHILD_WRITE = 3 };
+constexpr uint32_t CHILD_GRID_MIN = 2048;  // segments from which a level uses the grid form
+
+template <class KT, class WT>
+__device__ __forceinline__ void children_body(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
+                                              uint32_t level, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
+                                              Trav<KT> *trav, RunScalars *rs, const SetTab &sets, int phase,
+                                              uint64_t *blk) {
+    typedef typename KT::T K;
+    __shared__ uint64_t sh[33];
+    // launched right after a speculative pass: nothing to do while a segment
+    // of the level is still searching (the host runs more passes, then this)
+    if (rs->nactive != 0) return;
+    const bool multi = sets.count > 1;
+    uint64_t outc = 0, outv = 0;
+    uint64_t hmin = ~0ull;
+    const int nc = (coord + 1) % D;
+    // CHILD_ALL: one CTA walks every segment.  Levels with many segments use
+    // a grid of CTAs, one per 1024 segments, in three launches:
+    // CHILD_COUNT (each CTA's children and items into blk), CHILD_SCAN (one
+    // CTA: blk becomes exclusive offsets) and CHILD_WRITE.
+    uint32_t first = 0, stop = S;
+    if (phase == CHILD_COUNT || phase == CHILD_WRITE) {
+        first = blockIdx.x * blockDim.x;
+        stop = min(S, first + blockDim.x);
+        if (phase == CHILD_WRITE) {
+            outc = blk[2 * blockIdx.x];
+            outv = blk[2 * blockIdx.x + 1];
+        }
+    }
+    if (phase == CHILD_SCAN) {
+        const uint32_t nb = (S + 1023) / 1024;
+        for (uint32_t b0 = 0; b0 < nb; b0 += blockDim.x) {
+            const uint32_t b = b0 + threadIdx.x;
+            const uint64_t c = b < nb ? blk[2 * b] : 0, v = b < nb ? blk[2 * b + 1] : 0;
+            uint64_t tc, tv;
+            const uint64_t ci = block_exscan_u64(c, sh, tc);
+            const uint64_t vi = block_exscan_u64(v, sh, tv);
+            if (b < nb) {
+                blk[2 * b] = outc + ci;
+                blk[2 * b + 1] = outv + vi;
+            }
+            outc += tc;
+            outv += tv;
+        }
+        if (threadIdx.x == 0) {
+            rs->nsegs_next = outc;
+            rs->items_next = outv;
+            if (write) next_P[outc] = outv;
+        }
+        return;
+    }
+    for (uint32_t base = first; base < stop; base += blockDim.x) {
+        const uint32_t s = base + threadIdx.x;
+        Seg<KT> sg;
+        uint32_t nl = 0, nr = 0;
+        bool leaves = !write;  // the children are parts: no segments for them
+        if (s < S) {
+            sg = segs[s];
+            nl = sg.nleft;
+            if (nl > sg.n) {  // inconsistent split: report, and keep sizes in range
+                atomicOr(&rs->err, ERR_COUNT_MISMATCH);
+                nl = sg.n;
+            }
+            nr = sg.n - nl;
+            if (multi && sets.iters[sg.set] <= level + 1) leaves = true;  // the set's last level
+        }
+        uint64_t tc, tv;
+        const uint64_t ci = block_exscan_u64(leaves ? 0 : (nl > 0) + (nr > 0), sh, tc);
+        const uint64_t vi = block_exscan_u64(leaves ? 0 : (uint64_t)nl + nr, sh, tv);
+        if (phase == CHILD_COUNT) {
+            if (threadIdx.x == 0) {
+                blk[2 * blockIdx.x] = tc;
+                blk[2 * blockIdx.x + 1] = tv;
+            }
+            return;
+        }
+        if (s < stop) {
+            const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
+            if (leaves) {
+                uint64_t h = ~0ull;
+                if (nl > 0) h = hl;
+                if (nr > 0) h = hr < h ? hr : h;
+                if (multi)
+                    atomicMin((unsigned long long *)&sets.minheap[sg.set], (unsigned long long)h);
+                else
+                    hmin = h < hmin ? h : hmin;
+            }
+            if (trav) {
+                Trav<KT> t;
+                t.pivot = sg.pivot;
+                t.flags = (sg.state == SEG_ALLLEFT ? TRAV_ALLLEFT : 0u) | (nl > 0 ? TRAV_HAS_LEFT : 0u);
+                t.next = leaves ? sg.heap : outc + ci;
+                t.blo = t.bhi = 0.f;
+                if constexpr (KT::BAND) {
+                    const CutBounds cb = band_bounds(sg.pivot);
+                    t.blo = cb.lo;
+                    t.bhi = cb.hi;
+                }
+                trav[s] = t;
+            }
+            if (!leaves) {
+                segs[s].child = (uint32_t)(outc + ci);
+                uint64_t c = outc + ci;
+                const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
+                for (int side = 0; side < 2; ++side) {
+                    const uint32_t cn = side == 0 ? nl : nr;
+                    if (!cn) continue;
+                    Seg<KT> ch;
+                    ch.off = side == 0 ? sg.off : sg.off + nl;
+                    ch.voff = outv + vi + (side == 0 ? 0 : nl);
+                    ch.heap = side == 0 ? hl : hr;
+                    if (sg.wlx) {
+                        ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
+                        ch.sumx = SUMX_NONE;
+                    } else {
+                        // weight_left known only within bounds: the next
+                        // level's first pass sums the left child's items
+                        ch.sum = side == 0 ? 0 : sg.sum;
+                        ch.sumx = side == 0 ? SUMX_OWN : (nl > 0 ? SUMX_RIGHT : SUMX_NONE);
+                    }
+                    ch.exactw = 0;
+                    ch.wlx = 0;
+                    ch.pad2 = 0;
+#pragma unroll
+                    for (int l = 0; l < 4; ++l) ch.xq[l] = 0;
+                    ch.prev = ~0ull;
+                    ch.wl = 0;
+                    ch.n = cn;
+                    ch.nleft = 0;
+                    ch.state = SEG_ACTIVE;
+                    ch.steps = 0;
+                    ch.child = 0;
+                    ch.xstate = 0;
+                    ch.xkey = 0;
+                    ch.set = sg.set;
+                    ch.xcut = 0;
+                    ch.xmin = ~0ull;
+                    for (int d = 0; d < 3; ++d) {
+                        ch.bmin[d] = sg.bmin[d];
+                        ch.bmax[d] = sg.bmax[d];
+                    }
+                    if (side == 0)
+                        ch.bmax[coord] = sg.split_pos;
+                    else
+                        ch.bmin[coord] = sg.split_pos;
+                    ch.lo = ch.bmin[nc];
+                    ch.hi = ch.bmax[nc];
+                    ch.pivot = 0;
+                    ch.split_pos = 0;
+                    next[c] = ch;
+                    next_list[c] = (uint32_t)c;
+                    next_P[c] = ch.voff;
+                    ++c;
+                }
+            }
+        }
+        outc += tc;
+        outv += tv;
+    }
+    hmin = warp_min_u64(hmin);
+    if (!multi && (threadIdx.x & 31) == 0 && hmin != ~0ull)
+        atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
+    if (phase == CHILD_ALL && threadIdx.x == 0) {
+        rs->nsegs_next = outc;
+        rs->items_next = outv;
+        if (write) next_P[outc] = outv;
+    }
+}
+
+template <class KT, class WT>
+__global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
+                                                   uint32_t level, Seg<KT> *next, uint32_t *next_list,
+                                                   uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets,
+                                                   int phase, uint64_t *blk) {
+    children_body<KT, WT>(segs, S, coord, D, write, level, next, next_list, next_P, trav, rs, sets, phase, blk);
+}
+
+// The next level's segments built by the last CTA of a decide launch (levels
+// below CHILD_GRID_MIN segments, after the speculative pass).
+template <class KT>
+struct ChildArgs {
+    int on;
+    uint32_t S;
+    int coord, D, write;
+    uint32_t level;
+    Seg<KT> *next;
+    uint32_t *next_list;
+    uint64_t *next_P;
+    Trav<KT> *trav;
+    SetTab sets;
+};
+
 // Compacts the listed segments still searching into list2 with the exclusive
 // prefix P2 of their sizes.  One CTA.
 template <class KT>
@@ -1642,7 +1840,8 @@ template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
                                                   RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs,
-                                                  const int32_t *__restrict__ set_qb, uint32_t *list2, uint64_t *P2) {
+                                                  const int32_t *__restrict__ set_qb, uint32_t *list2, uint64_t *P2,
+                                                  ChildArgs<KT> ca) {
     __shared__ uint32_t s_last;
     // a speculative pass: the list the last scan left (the grid is an upper
     // bound); every CTA reads it before the last one overwrites it
@@ -1657,184 +1856,15 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
         __threadfence();
         scan_list_block<KT>(segs, list, flags, nlist, list2, P2, rs);
         if (threadIdx.x == 0) rs->decide_done = 0;
+        if (ca.on) {
+            __syncthreads();  // the scan's count (rs->nactive) is read below
+            children_body<KT, WT>(segs, ca.S, ca.coord, ca.D, ca.write, ca.level, ca.next, ca.next_list, ca.next_P,
+                                  ca.trav, rs, ca.sets, CHILD_ALL, nullptr);
+        }
     }
 }
 
 
-// Builds the next level's segments from the finished splits: left child
-// (heap 2h+1, sum = weight_left, bbox max[coord] = split_pos) and right child
-// (2h+2, sum - weight_left, bbox min[coord] = split_pos), empty children
-// dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
-// the smallest heap id among the children (the id offset, :698-702).
-enum : int { CHILD_ALL = 0, CHILD_COUNT = 1, CHILD_SCAN = 2, CHILD_WRITE = 3 };
-constexpr uint32_t CHILD_GRID_MIN = 2048;  // segments from which a level uses the grid form
-
-template <class KT, class WT>
-__global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
-                                                   uint32_t level, Seg<KT> *next, uint32_t *next_list,
-                                                   uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets,
-                                                   int phase, uint64_t *blk) {
-    typedef typename KT::T K;
-    __shared__ uint64_t sh[33];
-    // launched right after a speculative pass: nothing to do while a segment
-    // of the level is still searching (the host runs more passes, then this)
-    if (rs->nactive != 0) return;
-    const bool multi = sets.count > 1;
-    uint64_t outc = 0, outv = 0;
-    uint64_t hmin = ~0ull;
-    const int nc = (coord + 1) % D;
-    // CHILD_ALL: one CTA walks every segment.  Levels with many segments use
-    // a grid of CTAs, one per 1024 segments, in three launches:
-    // CHILD_COUNT (each CTA's children and items into blk), CHILD_SCAN (one
-    // CTA: blk becomes exclusive offsets) and CHILD_WRITE.
-    uint32_t first = 0, stop = S;
-    if (phase == CHILD_COUNT || phase == CHILD_WRITE) {
-        first = blockIdx.x * blockDim.x;
-        stop = min(S, first + blockDim.x);
-        if (phase == CHILD_WRITE) {
-            outc = blk[2 * blockIdx.x];
-            outv = blk[2 * blockIdx.x + 1];
-        }
-    }
-    if (phase == CHILD_SCAN) {
-        const uint32_t nb = (S + 1023) / 1024;
-        for (uint32_t b0 = 0; b0 < nb; b0 += blockDim.x) {
-            const uint32_t b = b0 + threadIdx.x;
-            const uint64_t c = b < nb ? blk[2 * b] : 0, v = b < nb ? blk[2 * b + 1] : 0;
-            uint64_t tc, tv;
-            const uint64_t ci = block_exscan_u64(c, sh, tc);
-            const uint64_t vi = block_exscan_u64(v, sh, tv);
-            if (b < nb) {
-                blk[2 * b] = outc + ci;
-                blk[2 * b + 1] = outv + vi;
-            }
-            outc += tc;
-            outv += tv;
-        }
-        if (threadIdx.x == 0) {
-            rs->nsegs_next = outc;
-            rs->items_next = outv;
-            if (write) next_P[outc] = outv;
-        }
-        return;
-    }
-    for (uint32_t base = first; base < stop; base += blockDim.x) {
-        const uint32_t s = base + threadIdx.x;
-        Seg<KT> sg;
-        uint32_t nl = 0, nr = 0;
-        bool leaves = !write;  // the children are parts: no segments for them
-        if (s < S) {
-            sg = segs[s];
-            nl = sg.nleft;
-            if (nl > sg.n) {  // inconsistent split: report, and keep sizes in range
-                atomicOr(&rs->err, ERR_COUNT_MISMATCH);
-                nl = sg.n;
-            }
-            nr = sg.n - nl;
-            if (multi && sets.iters[sg.set] <= level + 1) leaves = true;  // the set's last level
-        }
-        uint64_t tc, tv;
-        const uint64_t ci = block_exscan_u64(leaves ? 0 : (nl > 0) + (nr > 0), sh, tc);
-        const uint64_t vi = block_exscan_u64(leaves ? 0 : (uint64_t)nl + nr, sh, tv);
-        if (phase == CHILD_COUNT) {
-            if (threadIdx.x == 0) {
-                blk[2 * blockIdx.x] = tc;
-                blk[2 * blockIdx.x + 1] = tv;
-            }
-            return;
-        }
-        if (s < stop) {
-            const uint64_t hl = 2 * sg.heap + 1, hr = 2 * sg.heap + 2;
-            if (leaves) {
-                uint64_t h = ~0ull;
-                if (nl > 0) h = hl;
-                if (nr > 0) h = hr < h ? hr : h;
-                if (multi)
-                    atomicMin((unsigned long long *)&sets.minheap[sg.set], (unsigned long long)h);
-                else
-                    hmin = h < hmin ? h : hmin;
-            }
-            if (trav) {
-                Trav<KT> t;
-                t.pivot = sg.pivot;
-                t.flags = (sg.state == SEG_ALLLEFT ? TRAV_ALLLEFT : 0u) | (nl > 0 ? TRAV_HAS_LEFT : 0u);
-                t.next = leaves ? sg.heap : outc + ci;
-                t.blo = t.bhi = 0.f;
-                if constexpr (KT::BAND) {
-                    const CutBounds cb = band_bounds(sg.pivot);
-                    t.blo = cb.lo;
-                    t.bhi = cb.hi;
-                }
-                trav[s] = t;
-            }
-            if (!leaves) {
-                segs[s].child = (uint32_t)(outc + ci);
-                uint64_t c = outc + ci;
-                const typename WT::V sum = WT::from_bits(sg.sum), wl = WT::from_bits(sg.wl);
-                for (int side = 0; side < 2; ++side) {
-                    const uint32_t cn = side == 0 ? nl : nr;
-                    if (!cn) continue;
-                    Seg<KT> ch;
-                    ch.off = side == 0 ? sg.off : sg.off + nl;
-                    ch.voff = outv + vi + (side == 0 ? 0 : nl);
-                    ch.heap = side == 0 ? hl : hr;
-                    if (sg.wlx) {
-                        ch.sum = WT::bits(side == 0 ? wl : WT::sub(sum, wl));
-                        ch.sumx = SUMX_NONE;
-                    } else {
-                        // weight_left known only within bounds: the next
-                        // level's first pass sums the left child's items
-                        ch.sum = side == 0 ? 0 : sg.sum;
-                        ch.sumx = side == 0 ? SUMX_OWN : (nl > 0 ? SUMX_RIGHT : SUMX_NONE);
-                    }
-                    ch.exactw = 0;
-                    ch.wlx = 0;
-                    ch.pad2 = 0;
-#pragma unroll
-                    for (int l = 0; l < 4; ++l) ch.xq[l] = 0;
-                    ch.prev = ~0ull;
-                    ch.wl = 0;
-                    ch.n = cn;
-                    ch.nleft = 0;
-                    ch.state = SEG_ACTIVE;
-                    ch.steps = 0;
-                    ch.child = 0;
-                    ch.xstate = 0;
-                    ch.xkey = 0;
-                    ch.set = sg.set;
-                    ch.xcut = 0;
-                    ch.xmin = ~0ull;
-                    for (int d = 0; d < 3; ++d) {
-                        ch.bmin[d] = sg.bmin[d];
-                        ch.bmax[d] = sg.bmax[d];
-                    }
-                    if (side == 0)
-                        ch.bmax[coord] = sg.split_pos;
-                    else
-                        ch.bmin[coord] = sg.split_pos;
-                    ch.lo = ch.bmin[nc];
-                    ch.hi = ch.bmax[nc];
-                    ch.pivot = 0;
-                    ch.split_pos = 0;
-                    next[c] = ch;
-                    next_list[c] = (uint32_t)c;
-                    next_P[c] = ch.voff;
-                    ++c;
-                }
-            }
-        }
-        outc += tc;
-        outv += tv;
-    }
-    hmin = warp_min_u64(hmin);
-    if (!multi && (threadIdx.x & 31) == 0 && hmin != ~0ull)
-        atomicMin((unsigned long long *)&rs->min_heap, (unsigned long long)hmin);
-    if (phase == CHILD_ALL && threadIdx.x == 0) {
-        rs->nsegs_next = outc;
-        rs->items_next = outv;
-        if (write) next_P[outc] = outv;
-    }
-}
 
 // ---------------------------------------------------------------------------
 // k_reorder: stable two-way partition of every segment of the level, out of

@@ -240,6 +240,23 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             return (int)COUPE_ERR_OK;
         };
         const unsigned decide_grid = (unsigned)((S + NWARPS - 1) / NWARPS);
+        // levels below CHILD_GRID_MIN segments build their children in the
+        // last CTA of the speculative decide (when no segment is searching)
+        const bool fuse = S < CHILD_GRID_MIN;
+        ChildArgs<KT> no_ch;
+        std::memset(&no_ch, 0, sizeof(no_ch));
+        ChildArgs<KT> ch = no_ch;
+        ch.on = fuse ? 1 : 0;
+        ch.S = (uint32_t)S;
+        ch.coord = coord;
+        ch.D = D;
+        ch.write = last ? 0 : 1;
+        ch.level = (uint32_t)L;
+        ch.next = B.segs[snext];
+        ch.next_list = B.list[0];
+        ch.next_P = B.P[0];
+        ch.trav = trav_l;
+        ch.sets = sets;
         const uint64_t decide_bytes = S * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord));
         // First pass over every point of the level, its decisions, and the
         // list of segments still searching (list[1]).
@@ -254,7 +271,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         bytes += V * (sk + sw);
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
-                                                                 B.flags, B.rs, 0, set_fs, set_qb, B.list[1], B.P[1]));
+                                                                 B.flags, B.rs, 0, set_fs, set_qb, B.list[1], B.P[1],
+                                                                 no_ch));
         // A speculative second pass over list[1] without asking the host how
         // long it is: its kernels read the count the scan left and return at
         // once when no segment is searching.  The next scan leaves list[0].
@@ -264,9 +282,9 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         ++st->hist_passes;
         CG_LAUNCH(KID_DECIDE, decide_bytes,
                   k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
-                                                                 B.rs, 1, set_fs, set_qb, B.list[0], B.P[0]));
+                                                                 B.rs, 1, set_fs, set_qb, B.list[0], B.P[0], ch));
         // k_children returns at once if a segment is still searching
-        if (!last) {
+        if (!last && !fuse) {
             const int rc_ = children();
             if (rc_ != COUPE_ERR_OK) return rc_;
         }
@@ -294,7 +312,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
                       k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
                           segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs, set_qb,
-                          B.list[li ^ 1], B.P[li ^ 1]));
+                          B.list[li ^ 1], B.P[li ^ 1], no_ch));
             li ^= 1;
             CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
             CG_CK(cudaStreamSynchronize(s));
@@ -304,7 +322,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             err_level = (int)L;
             break;
         }
-        if (last || more) {
+        if ((last && !fuse) || more) {
             const int rc_ = children();
             if (rc_ != COUPE_ERR_OK) return rc_;
         }
