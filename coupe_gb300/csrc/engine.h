@@ -51,7 +51,7 @@ constexpr uint64_t TRAV_MAX_ENTRIES = 1ull << 22;
 
 // Kernel kinds timed by the optional per-launch profiler.
 enum KernelId {
-    KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_SCAN, KID_CHILDREN, KID_REORDER,
+    KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_CHILDREN, KID_REORDER,
     KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_COUNT
 };
 const char *kernel_name(int id);
