@@ -617,8 +617,7 @@ static __global__ void k_sets_init(SetTab sets) {
 // ---------------------------------------------------------------------------
 template <class KT, bool WARP = false>
 __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT::C hi, int nbk,
-                                                  typename KT::C *cuts, float *cb_lo = nullptr,
-                                                  float *cb_hi = nullptr) {
+                                                  typename KT::C *cuts, float4 *cbb = nullptr) {
     typedef typename KT::C K;
     // One depth of the tree at a time: node (d, p) at in-order rank
     // r = (2p + 1) h - 1, h = 2^(nbk-1-d), is the midpoint of the cuts at ranks
@@ -636,10 +635,29 @@ __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT
             const K b = r + h >= nb - 1 ? hi : cuts[r + h];
             cuts[r] = KT::cmid(a, b);
             if constexpr (KT::BAND) {
-                // the band form also needs each cut's f32 bounds
+                // the band form also needs each cut's f32 bounds (bin r's
+                // upper edge and band)
                 const CutBounds cb = band_bounds(cuts[r]);
-                cb_lo[r] = cb.lo;
-                cb_hi[r] = cb.hi;
+                cbb[r].y = cb.hi;
+                cbb[r].z = cb.lo;
+                cbb[r].w = 1.f;
+            }
+        }
+        if (WARP)
+            __syncwarp();
+        else
+            __syncthreads();
+    }
+    if constexpr (KT::BAND) {
+        // bin b's record: (upper bound of cut b-1, upper bound of cut b,
+        // lower bound of cut b, 1 when cut b exists); one 16-byte load
+        // checks a guessed bin
+        for (int b = tr; b < nb; b += TS) {
+            cbb[b].x = b > 0 ? cbb[b - 1].y : -INFINITY;
+            if (b == nb - 1) {
+                cbb[b].y = INFINITY;
+                cbb[b].z = INFINITY;
+                cbb[b].w = 0.f;
             }
         }
         if (WARP)
@@ -693,27 +711,28 @@ __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT:
 // upper bound lies below the key are certainly passed; if the next cut's
 // lower bound does not exceed the key, the f64 code decides from there.
 template <class KT>
-__device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const float *cb_lo, const float *cb_hi, int nb,
+__device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const float4 *cbb, int nb,
                                         const BinGuess &g, bool &in_band) {
     int b;
     if (g.fast) {
         float f = (k - g.lo) * g.scale;
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
         b = __float2int_rz(f);
-        while (b > 0 && !(k > cb_hi[b - 1])) --b;
-        while (b < nb - 1 && k > cb_hi[b]) ++b;
     } else {
         int l = 0, r = nb - 1;
         while (l < r) {
             const int m = (l + r) >> 1;
-            if (k > cb_hi[m])
+            if (k > cbb[m].y)
                 l = m + 1;
             else
                 r = m;
         }
         b = l;
     }
-    in_band = b < nb - 1 && !(k < cb_lo[b]);  // cut b's band: finish with bin_band_exact
+    float4 q = cbb[b];
+    while (b > 0 && !(k > q.x)) q = cbb[--b];
+    while (b < nb - 1 && k > q.y) q = cbb[++b];
+    in_band = q.w != 0.f && !(k < q.z);  // cut b's band: finish with bin_band_exact
     return b;
 }
 // The bin from cut b on, from the f64 code.
@@ -766,7 +785,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     constexpr int HNB = 1 << hist_max_nbk<WT>();
     constexpr int BNB = KT::BAND ? HNB : 1;
     __shared__ CK cuts[HNB];
-    __shared__ float cb_lo[BNB], cb_hi[BNB];  // band form: f32 bounds of the cuts
+    __shared__ float4 cbb[BNB];  // band form: f32 bounds of each bin (see build_sorted_cuts)
     __shared__ uint64_t sw[HNB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
     __shared__ uint32_t scnt[HNB];
     __shared__ O sinv[HNB];
@@ -804,12 +823,12 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         const bool spk = packed_all || apx;
         const bool accx = L > 1 && sg.sumx != SUMX_NONE;
         CK *const wc = cuts + warp * SNB;
-        float *const wlo = cb_lo + (KT::BAND ? warp * SNB : 0), *const whi = cb_hi + (KT::BAND ? warp * SNB : 0);
+        float4 *const wcb = cbb + (KT::BAND ? warp * SNB : 0);
         uint64_t *const wsw = sw + warp * SNB * L;
         uint32_t *const wcnt = scnt + warp * SNB;
         O *const winv = sinv + warp * SNB;
         const CK lo = sg.lo, hi = sg.hi;
-        build_sorted_cuts<KT, true>(lo, hi, nbk, wc, wlo, whi);
+        build_sorted_cuts<KT, true>(lo, hi, nbk, wc, wcb);
         for (int i = lane; i < NB; i += 32) {
             wcnt[i] = 0;
             winv[i] = 0;
@@ -852,7 +871,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             int bin;
             if constexpr (KT::BAND) {
                 bool in_band;
-                bin = bin_band<KT>(kv, wc, wlo, whi, NB, g, in_band);
+                bin = bin_band<KT>(kv, wc, wcb, NB, g, in_band);
                 const bool pend = sg.xstate == X_PENDING && KT::ord(kv) == sg.xkey;
                 if (in_band || pend) {
                     // the key's bin is a lower bound; the f64 coordinate decides
@@ -981,7 +1000,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         const uint64_t a = sg.off + (pos - P[k]), b = a + (pe - pos);
         const CK lo = sg.lo, hi = sg.hi;
         __syncthreads();
-        if ((int)s != cur_s) build_sorted_cuts<KT>(lo, hi, nbk, cuts, cb_lo, cb_hi);
+        if ((int)s != cur_s) build_sorted_cuts<KT>(lo, hi, nbk, cuts, cbb);
         cur_s = (int)s;
         for (int i = threadIdx.x; i < NB; i += BLOCK) {
             scnt[i] = 0;
@@ -1036,7 +1055,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                     return;
                 }
                 bool unused;
-                const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cb_lo, cb_hi, NB, g, unused), c, cuts, NB);
+                const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cbb, NB, g, unused), c, cuts, NB);
                 if (packed) {
                     atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
                 } else {
@@ -1084,7 +1103,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                         // their neighbours inside it; edge-bin sums stay in
                         // registers (most keys once the interval has narrowed)
                         bool in_band;
-                        const int bin = bin_band<KT>(kv[i], cuts, cb_lo, cb_hi, NB, g, in_band);
+                        const int bin = bin_band<KT>(kv[i], cuts, cbb, NB, g, in_band);
                         if (in_band) {
                             slow |= 1u << i;
                             continue;
