@@ -32,6 +32,13 @@ struct RunArgs {
     uint64_t nsets = 1;
     const uint64_t *set_off = nullptr;
     const uint32_t *set_iters = nullptr;
+    // host calls: the weights are still uploading until this event (the
+    // weight kernels wait for it; the key conversion does not)
+    cudaEvent_t weights_ready = nullptr;
+    // host calls with a pinned id buffer: its device-mapped address; the
+    // traversal then writes the ids there directly and sets *ids_on_host
+    uint64_t *ids_host = nullptr;
+    bool *ids_on_host = nullptr;
 };
 
 // Process-wide tuning knobs (coupe_gpu_set_option).  They change how the
@@ -84,6 +91,8 @@ struct DevCtx {
     int dev = -1;
     int sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // host calls: the weight upload
+    cudaEvent_t ev_pts = nullptr, ev_w = nullptr;
     void *ws = nullptr;
     size_t ws_cap = 0;
     void *h_pinned = nullptr;  // pinned host scratch for scalar read-backs

@@ -177,8 +177,15 @@ coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const c
         for (uintptr_t i = 0; i < n; ++i) fetch(weights, i, wsz, h + i * wsz);
         src_w = h;
     }
+    // The points go first; the weights follow on a second stream, so that
+    // the key conversion runs while they upload (the weight kernels wait for
+    // them).
     if ((e = cudaMemcpyAsync(d_pts, src_p, pbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess) {
+        (e = cudaEventRecord(C->ev_pts, s)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(C->stream2, C->ev_pts, 0)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, C->stream2)) != cudaSuccess ||
+        (e = cudaEventRecord(C->ev_w, C->stream2)) != cudaSuccess) {
+        cudaStreamSynchronize(C->stream2);
         int rc = cg::cuda_fail(e, "host to device copy", &t_err);
         return (coupe_err)rc;
     }
@@ -193,6 +200,17 @@ coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const c
     a.tolerance = tolerance;
     a.mode = mode;
     a.stream = s;
+    a.weights_ready = C->ev_w;
+    // a pinned id buffer: the ids are written into it by the last kernel
+    static_assert(sizeof(uintptr_t) == sizeof(uint64_t), "64-bit uintptr_t expected");
+    bool ids_on_host = false;
+    void *mapped = nullptr;
+    if (is_pinned(partition) && cudaHostGetDevicePointer(&mapped, partition, 0) == cudaSuccess && mapped) {
+        a.ids_host = (uint64_t *)mapped;
+        a.ids_on_host = &ids_on_host;
+    } else {
+        cudaGetLastError();
+    }
     int rc = COUPE_ERR_OK;
     if (rib) {
         double M[9];
@@ -203,13 +221,14 @@ coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const c
         }
     }
     if (rc == COUPE_ERR_OK) rc = cg::run_rcb(*C, a, &t_stats, &err);
+    cudaStreamSynchronize(C->stream2);  // the weight upload has ended (it has on success)
     if (rc != COUPE_ERR_OK) {
         t_err = err;
         return (coupe_err)rc;
     }
-    static_assert(sizeof(uintptr_t) == sizeof(uint64_t), "64-bit uintptr_t expected");
-    if ((e = cudaMemcpyAsync(partition, d_part, obytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    if (!ids_on_host && (e = cudaMemcpyAsync(partition, d_part, obytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "device to host copy", &t_err);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess)
         return (coupe_err)cg::cuda_fail(e, "device to host copy", &t_err);
     return COUPE_ERR_OK;
 }

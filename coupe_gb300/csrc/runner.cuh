@@ -335,10 +335,17 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             }
         }
         if (last) {
+            // a host call's pinned id buffer takes the traversal's writes
+            // directly (coalesced, over the host link) instead of a copy after
+            uint64_t *ids = a.d_part;
+            if (a.ids_host && !index_path) {
+                ids = a.ids_host;
+                if (a.ids_on_host) *a.ids_on_host = true;
+            }
             if (multi) {
                 CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                           k_traverse_sets<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, lv, B.keys[0][0], B.keys[0][1],
-                                                                            B.keys[0][2], n, a.d_part, sets, bs));
+                                                                            B.keys[0][2], n, ids, sets, bs));
                 bytes += n * (D * sk + 8);
             } else if (index_path) {
                 CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
@@ -352,12 +359,12 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                     CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                               k_traverse_smem<D, KT><<<g_stream, BLOCK, tsm, s>>>(
                                   B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
-                                  B.keys[0][2], n, a.d_part, B.rs, bs));
+                                  B.keys[0][2], n, ids, B.rs, bs));
                 } else {
                     CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                               k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters,
                                                                            B.keys[0][0], B.keys[0][1], B.keys[0][2],
-                                                                           n, a.d_part, B.rs, bs));
+                                                                           n, ids, B.rs, bs));
                 }
                 bytes += n * (D * sk + 8);
             }
@@ -569,6 +576,7 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
               k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
                                                           B.rs, sets));
     const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
+    if (a.weights_ready) CG_CK(cudaStreamWaitEvent(s, a.weights_ready, 0));
     if (WT::LIMBS > 1) {
         CG_LAUNCH(KID_WABS, n * sw, k_wabs_max<<<g_stream, BLOCK, 0, s>>>((const double *)w_in, n, B.rs, sets));
         if (multi) CG_LAUNCH(KID_WABS, 0, k_set_fs<<<(unsigned)((nsets + 255) / 256), 256, 0, s>>>(sets, B.rs));

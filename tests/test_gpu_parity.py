@@ -466,3 +466,36 @@ def test_small_segments_binned_per_warp(coupe, oracle_mod, mode, nbk, exact):
     finally:
         coupe.set_option("max_nbk", 10)
         coupe.set_option("exact_f64_hist", 0)
+
+
+def test_pinned_host_buffers(coupe, oracle_mod):
+    """Host calls with pinned (page-locked) buffers: the weights upload
+    overlaps the key conversion and the ids are written straight into the
+    pinned id buffer (or copied after, on the index path).  Same ids as with
+    pageable buffers and as the oracle."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(91)
+    n = 300_000
+    for dim, wk in ((3, "i64"), (2, "f64")):
+        pts, w = _make(n, dim, wk, 91 + dim)
+        pp = torch.from_numpy(pts).pin_memory().numpy()
+        pw = torch.from_numpy(w).pin_memory().numpy()
+        for knobs in ({}, {"force_index_path": 1}):
+            old = {k: coupe.get_option(k) for k in knobs}
+            try:
+                for k, v in knobs.items():
+                    coupe.set_option(k, v)
+                for mode in ("ref32", "f32key_f64band"):
+                    want, _ = oracle_mod.rcb(pts, w, 9, 0.01, mode=_oracle_mode(mode))
+                    ids = torch.zeros(n, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+                    ids[:] = 12345
+                    coupe.Rcb(iter_count=9, tolerance=0.01, mode=mode).partition(ids, (pp, pw))
+                    assert np.array_equal(ids, want), (dim, wk, knobs, mode)
+                    ids2 = torch.zeros(n, dtype=torch.int64).pin_memory().numpy().view(np.uint64)
+                    coupe.Rib(iter_count=5, tolerance=0.02, mode=mode).partition(ids2, (pp, pw))
+                    ref = np.zeros(n, dtype=np.uint64)
+                    coupe.Rib(iter_count=5, tolerance=0.02, mode=mode).partition(ref, (pts, w))
+                    assert np.array_equal(ids2, ref)
+            finally:
+                for k, v in old.items():
+                    coupe.set_option(k, v)
