@@ -1279,8 +1279,10 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
 // Builds the next level's segments from the finished splits: left child
 // (heap 2h+1, sum = weight_left, bbox max[coord] = split_pos) and right child
 // (2h+2, sum - weight_left, bbox min[coord] = split_pos), empty children
-// dropped (recursive_bisection.rs:586-588, 606-641).  One CTA.  Also records
-// the smallest heap id among the children (the id offset, :698-702).
+// dropped (recursive_bisection.rs:586-588, 606-641).  Run by one CTA (the
+// k_children kernel, or the last CTA of a decide launch) or, for wide
+// levels, by a grid in three phases.  Also records the smallest heap id
+// among the children (the id offset, :698-702).
 enum : int { CHILD_ALL = 0, CHILD_COUNT = 1, CHILD_SCAN = 2, CHILD_WRITE = 3 };
 constexpr uint32_t CHILD_GRID_MIN = 2048;  // segments from which a level uses the grid form
 
