@@ -2323,7 +2323,8 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
 
 // ---------------------------------------------------------------------------
 // k_traverse_smem: k_traverse for a table that fits in shared memory (the
-// usual case: 1023 splits for 1024 parts).  The table is staged as arrays:
+// usual case: 1023 splits for 1024 parts), REF32 and F64 forms (the band
+// form has k_traverse_band).  The table is staged as arrays:
 // pivots, one 32-bit word per split (index of the first child in the next
 // level | all-left flag << 30 | has-left flag << 31) and the heap ids of the
 // last level.  Each thread walks TRAV_ILP items at once so that their
@@ -2437,6 +2438,125 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
 // to the smallest heap id of its set.  Items of a set with iter_count 0 get
 // id 0.  Each CTA walks one contiguous range of items (few sets, so their
 // splits stay in L1), TRAV_ILP items per thread at once.
+// ---------------------------------------------------------------------------
+// k_traverse_band: the band form's k_traverse_smem.  One 16-byte record per
+// split holds what the walk reads at every level: the split's f32 bounds
+// RD32(pivot) <= RU32(pivot) and the word of k_traverse_smem.  The records of
+// a thread's TRAV_ILP items are loaded before any compare, and a key between
+// the bounds (rare) reads its f64 coordinate and the split's f64 pivot from
+// the global table after the others are compared.  The next items' keys load
+// during each walk.
+// ---------------------------------------------------------------------------
+struct __align__(16) BandNode {
+    float lo, hi;
+    uint32_t nx, pad;
+};
+
+__host__ __device__ constexpr size_t trav_band_smem_bytes(uint64_t total, uint64_t n_last) {
+    return total * sizeof(BandNode) + n_last * sizeof(uint64_t);
+}
+
+template <int D>
+__global__ void __launch_bounds__(BLOCK) k_traverse_band(const Trav<KeyBand> *__restrict__ trav, uint32_t total,
+                                                         LevelOffsets lv, int levels, const float *__restrict__ k0,
+                                                         const float *__restrict__ k1, const float *__restrict__ k2,
+                                                         uint64_t n, uint64_t *__restrict__ part,
+                                                         const RunScalars *rs, BandSrc bs) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ uint32_t s_off[MAX_TRAV_LEVELS];
+    const uint32_t off_last = (uint32_t)lv.off[levels - 1];
+    BandNode *s_node = (BandNode *)dsm;                   // [total]
+    uint64_t *s_heap = (uint64_t *)(s_node + total);      // [total - off_last]
+    for (uint32_t j = threadIdx.x; j < total; j += BLOCK) {
+        const Trav<KeyBand> t = trav[j];
+        BandNode nd;
+        nd.lo = t.blo;
+        nd.hi = t.bhi;
+        nd.nx = ((t.flags & TRAV_ALLLEFT) ? TRAV_NX_ALLLEFT : 0u) | ((t.flags & TRAV_HAS_LEFT) ? TRAV_NX_HASLEFT : 0u);
+        if (j < off_last) nd.nx |= (uint32_t)t.next & TRAV_NX_INDEX;
+        nd.pad = 0;
+        s_node[j] = nd;
+        if (j >= off_last) s_heap[j - off_last] = t.next;
+    }
+    for (int L = threadIdx.x; L < levels; L += BLOCK) s_off[L] = (uint32_t)lv.off[L];
+    __syncthreads();
+    const uint64_t hmin = rs->min_heap;
+    const uint64_t step = (uint64_t)gridDim.x * BLOCK * TRAV_ILP;
+    auto load_keys = [&](uint64_t b0, float (*kk)[D]) {
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = b0 + (uint64_t)k * BLOCK;
+            if (i < n) {
+                kk[k][0] = k0[i];
+                kk[k][1] = k1[i];
+                if (D == 3) kk[k][D - 1] = k2[i];
+            } else {
+#pragma unroll
+                for (int d = 0; d < D; ++d) kk[k][d] = 0.0f;
+            }
+        }
+    };
+    float key[TRAV_ILP][D];
+    uint64_t base = (uint64_t)blockIdx.x * BLOCK * TRAV_ILP + threadIdx.x;
+    load_keys(base, key);
+    for (; base < n; base += step) {
+        float nxt[TRAV_ILP][D];
+        load_keys(base + step, nxt);
+        uint32_t seg[TRAV_ILP];
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) seg[k] = 0;
+        // -1 left, 1 right (band_side; the f64 coordinate decides in the band)
+        auto sides = [&](const BandNode *nd, uint32_t o, int c, int *sd) {
+            bool band = false;
+#pragma unroll
+            for (int k = 0; k < TRAV_ILP; ++k) {
+                const float kc = c == 0 ? key[k][0] : (c == 1 ? key[k][1] : key[k][D - 1]);
+                sd[k] = (nd[k].nx & TRAV_NX_ALLLEFT) ? -1 : band_side(kc, CutBounds{nd[k].lo, nd[k].hi});
+                band |= sd[k] == 0;
+            }
+            if (band) {
+#pragma unroll 1
+                for (int k = 0; k < TRAV_ILP; ++k) {
+                    if (sd[k] != 0) continue;
+                    const uint64_t i = base + (uint64_t)k * BLOCK;
+                    sd[k] = (i < n && KeyF64::lt(band_code(bs, i, c), trav[o + seg[k]].pivot)) ? -1 : 1;
+                }
+            }
+        };
+        int c = 0;
+        for (int L = 0; L + 1 < levels; ++L) {
+            const uint32_t o = s_off[L];
+            BandNode nd[TRAV_ILP];
+#pragma unroll
+            for (int k = 0; k < TRAV_ILP; ++k) nd[k] = s_node[o + seg[k]];
+            int sd[TRAV_ILP];
+            sides(nd, o, c, sd);
+#pragma unroll
+            for (int k = 0; k < TRAV_ILP; ++k)
+                seg[k] = (nd[k].nx & TRAV_NX_INDEX) + ((sd[k] > 0 && (nd[k].nx & TRAV_NX_HASLEFT)) ? 1u : 0u);
+            c = c + 1 == D ? 0 : c + 1;
+        }
+        BandNode nd[TRAV_ILP];
+        uint64_t h[TRAV_ILP];
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            nd[k] = s_node[off_last + seg[k]];
+            h[k] = s_heap[seg[k]];
+        }
+        int sd[TRAV_ILP];
+        sides(nd, off_last, c, sd);
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k) {
+            const uint64_t i = base + (uint64_t)k * BLOCK;
+            if (i < n) part[i] = 2 * h[k] + (sd[k] < 0 ? 1 : 2) - hmin;
+        }
+#pragma unroll
+        for (int k = 0; k < TRAV_ILP; ++k)
+#pragma unroll
+            for (int d = 0; d < D; ++d) key[k][d] = nxt[k][d];
+    }
+}
+
 // ---------------------------------------------------------------------------
 template <int D, class KT>
 __global__ void __launch_bounds__(BLOCK) k_traverse_sets(const Trav<KT> *__restrict__ trav, LevelOffsets lv,

@@ -161,8 +161,13 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     uint64_t bytes = R0.bytes;
     const int nbk_max = std::min(hist_max_nbk<WL>(), std::max(1, tu.max_nbk));
     const size_t r_smem = reorder_smem<D, KT, WL>(carry);
-    CG_CK(cudaFuncSetAttribute((const void *)k_traverse_smem<D, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)TRAV_SMEM_MAX));
+    if constexpr (KT::BAND) {
+        CG_CK(cudaFuncSetAttribute((const void *)k_traverse_band<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)TRAV_SMEM_MAX));
+    } else {
+        CG_CK(cudaFuncSetAttribute((const void *)k_traverse_smem<D, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)TRAV_SMEM_MAX));
+    }
     const void *reorder_fn = carry ? (const void *)k_reorder<D, KT, WL, true> : (const void *)k_reorder<D, KT, WL, false>;
     CG_CK(cudaFuncSetAttribute(reorder_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem));
     const int g_reorder = occupancy_grid(reorder_fn, C.sms, BLOCK, r_smem);
@@ -354,12 +359,23 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                 bytes += n * (sk + (ic ? 4 : 0) + 8);
             } else {
                 const uint64_t n_last = trav_used - lv.off[iters - 1];
-                const size_t tsm = trav_smem_bytes<KT>(trav_used, n_last);
+                const size_t tsm = KT::BAND ? trav_band_smem_bytes(trav_used, n_last)
+                                            : trav_smem_bytes<KT>(trav_used, n_last);
                 if (tsm <= TRAV_SMEM_MAX) {
-                    CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
-                              k_traverse_smem<D, KT><<<g_stream, BLOCK, tsm, s>>>(
-                                  B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
-                                  B.keys[0][2], n, ids, B.rs, bs));
+                    if constexpr (KT::BAND) {
+                        // one resident wave: each CTA stages the table once
+                        const int g_trav = std::min<int>(
+                            g_stream, occupancy_grid((const void *)k_traverse_band<D>, C.sms, BLOCK, tsm));
+                        CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                                  k_traverse_band<D><<<g_trav, BLOCK, tsm, s>>>(
+                                      B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
+                                      B.keys[0][2], n, ids, B.rs, bs));
+                    } else {
+                        CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
+                                  k_traverse_smem<D, KT><<<g_stream, BLOCK, tsm, s>>>(
+                                      B.trav, (uint32_t)trav_used, lv, (int)iters, B.keys[0][0], B.keys[0][1],
+                                      B.keys[0][2], n, ids, B.rs, bs));
+                    }
                 } else {
                     CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                               k_traverse<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, trav_used, lv, (int)iters,
