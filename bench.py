@@ -294,11 +294,40 @@ def main():
         t_e2e = float(t.item())
     e2e_ok = bool((ho == ids_by_mode[headline]).all())
 
+    # the partition's imbalance (coupe::imbalance) on the device: the part
+    # loads of the headline ids, one pass over 16 B per point, then the
+    # O(parts) rest on the host; timed per call and per kernel
+    P = 1 << iters
+    dids = torch.from_numpy(ids_by_mode[headline].view(np.int64)).to(dev)
+    for _ in range(args.warmup):
+        imb = coupe.imbalance_device(P, dids, w)
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        imb = coupe.imbalance_device(P, dids, w)
+    ev1.record(stream)
+    barrier()
+    t_imb = ev0.elapsed_time(ev1) / args.steps
+    coupe.profile(True)
+    for _ in range(args.steps):
+        coupe.imbalance_device(P, dids, w)
+    torch.cuda.synchronize()
+    kl = coupe.profile_read().get("k_part_loads", {"ms": 0.0, "bytes": 0, "launches": 1})
+    coupe.profile(False)
+    k_ms = kl["ms"] / max(1, kl["launches"])
+    imbalance = {"value": imb, "parts": P, "ms_per_call": round(t_imb, 4), "kernel_us": round(1e3 * k_ms, 1),
+                 "kernel_GBps": round(kl["bytes"] / max(1, kl["launches"]) / (k_ms / 1e3) / 1e9, 1) if k_ms else None}
+
     cpu = None
     parity = {}
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu, cpu_ids = cpu_baseline(pts_h, w_h, cfg)
         parity["ref32_vs_oracle_mismatches"] = int((cpu_ids != ids_by_mode["ref32"]).sum())
+        import oracle  # the checker (cpu_baseline put it on the path)
+        t0 = time.perf_counter()
+        imb_cpu = oracle.imbalance(P, ids_by_mode[headline], w_h)
+        imbalance["cpu_oracle_ms"] = round(1e3 * (time.perf_counter() - t0), 1)
+        parity["imbalance_equals_oracle"] = bool(imb_cpu == imb)
     if "f32key_f64band" in ids_by_mode:
         parity["band_vs_f64_mismatches"] = int((ids_by_mode["f32key_f64band"] != ids_by_mode["f64"]).sum())
     parity["e2e_ids_equal_device_ids"] = e2e_ok
@@ -328,6 +357,7 @@ def main():
                 "kernel_us_per_step": {m: {k: round(1e3 * v["ms"] / args.steps, 1) for k, v in pr.items()}
                                        for m, pr in by_mode.items()}},
         "parity": parity,
+        "imbalance": imbalance,
         "clocks": clocks.summary() if clocks else None,
     }
     if "f32key_f64band" in results:

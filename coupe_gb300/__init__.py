@@ -40,6 +40,7 @@ EXPORTED = [
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
     "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
+    "coupe_gpu_parts_load", "coupe_gpu_imbalance", "coupe_gpu_parts_load_device", "coupe_gpu_imbalance_device",
 ]
 
 
@@ -125,6 +126,14 @@ def lib():
     L.coupe_gpu_kernel_name.restype = ctypes.c_char_p
     L.coupe_gpu_f64_to_f32.argtypes = [vp, vp, u64, vp]
     L.coupe_gpu_f64_to_f32.restype = i32
+    L.coupe_gpu_parts_load.argtypes = [vp, u64, vp, vp]
+    L.coupe_gpu_parts_load.restype = i32
+    L.coupe_gpu_imbalance.argtypes = [u64, vp, vp, ctypes.POINTER(dbl)]
+    L.coupe_gpu_imbalance.restype = i32
+    L.coupe_gpu_parts_load_device.argtypes = [vp, u64, i32, vp, u64, vp, vp]
+    L.coupe_gpu_parts_load_device.restype = i32
+    L.coupe_gpu_imbalance_device.argtypes = [u64, vp, u64, i32, vp, ctypes.POINTER(dbl), vp]
+    L.coupe_gpu_imbalance_device.restype = i32
     L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     L.coupe_gpu_set_option.restype = i32
     L.coupe_gpu_get_option.argtypes = [ctypes.c_char_p]
@@ -304,6 +313,110 @@ def autotune_device(part_ids, points, weights, set_offsets, iter_counts, toleran
                                   ctypes.byref(best))
     _check(rc)
     return best.as_dict()
+
+
+# ---------------------------------------------------------------------------
+# coupe::imbalance (coupe/src/imbalance.rs): part loads and the imbalance
+# metrics computed from them.
+# ---------------------------------------------------------------------------
+def _loads_dtype(wt):
+    return {COUPE_INT: np.int32, COUPE_INT64: np.int64, COUPE_DOUBLE: np.float64}[wt]
+
+
+def _host_ids(partition):
+    ids = np.ascontiguousarray(np.asarray(partition))
+    if ids.dtype != np.uint64:
+        ids = ids.astype(np.uint64)
+    return ids
+
+
+def compute_parts_load(partition, num_parts, weights):
+    """Load of each part (compute_parts_load, imbalance.rs:14-39) through
+    coupe_gpu_parts_load: an array of num_parts values of the weights' type.
+    A part id >= num_parts raises CoupeError (coupe panics)."""
+    ids = _host_ids(partition)
+    w = _as_weights(weights, len(ids))
+    if len(w) != len(ids):
+        raise CoupeError(ERR_LEN_MISMATCH)
+    wt = _weight_type(w)
+    out = np.zeros(num_parts, dtype=_loads_dtype(wt))
+    L = lib()
+    dw = L.coupe_data_array(len(w), wt, w.ctypes.data)
+    try:
+        rc = L.coupe_gpu_parts_load(ids.ctypes.data, num_parts, dw, out.ctypes.data)
+    finally:
+        L.coupe_data_free(dw)
+    _check(rc)
+    return out
+
+
+def imbalance(num_parts, partition, weights):
+    """coupe::imbalance::imbalance (imbalance.rs:41-77) through
+    coupe_gpu_imbalance: max over parts of (load - ideal) / ideal."""
+    ids = _host_ids(partition)
+    w = _as_weights(weights, len(ids))
+    if len(w) != len(ids):
+        raise CoupeError(ERR_LEN_MISMATCH)
+    out = ctypes.c_double(0.0)
+    L = lib()
+    dw = L.coupe_data_array(len(w), _weight_type(w), w.ctypes.data)
+    try:
+        rc = L.coupe_gpu_imbalance(num_parts, ids.ctypes.data, dw, ctypes.byref(out))
+    finally:
+        L.coupe_data_free(dw)
+    _check(rc)
+    return out.value
+
+
+def max_imbalance(num_parts, partition, weights):
+    """coupe::imbalance::max_imbalance (imbalance.rs:94-105): largest load
+    minus smallest load, in the weights' type (0 without parts)."""
+    loads = compute_parts_load(partition, num_parts, weights)
+    if len(loads) == 0:
+        return loads.dtype.type(0)
+    with np.errstate(over="ignore"):
+        return loads.max() - loads.min()
+
+
+def imbalance_target(targets, partition, weights):
+    """coupe::imbalance::imbalance_target (imbalance.rs:79-92): the largest
+    load - target over the parts (len(targets) parts; 0 without parts)."""
+    t = np.asarray(targets)
+    loads = compute_parts_load(partition, len(t), weights)
+    if len(loads) == 0:
+        return loads.dtype.type(0)
+    with np.errstate(over="ignore"):
+        return (loads - t.astype(loads.dtype)).max()
+
+
+def _device_weights(weights):
+    import torch
+    return {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+
+
+def parts_load_device(part_ids, weights, num_parts, stream=None):
+    """compute_parts_load on CUDA tensors (part_ids int64/uint64 (N,),
+    weights int32/int64/float64 (N,)); returns a host numpy array."""
+    import torch
+    wt = _device_weights(weights)
+    out = np.zeros(num_parts, dtype=_loads_dtype(wt))
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_parts_load_device(_ptr(part_ids), part_ids.numel(), wt, _ptr(weights), num_parts,
+                                           out.ctypes.data, ctypes.c_void_p(s))
+    _check(rc)
+    return out
+
+
+def imbalance_device(num_parts, part_ids, weights, stream=None):
+    """coupe::imbalance::imbalance on CUDA tensors."""
+    import torch
+    wt = _device_weights(weights)
+    out = ctypes.c_double(0.0)
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_imbalance_device(num_parts, _ptr(part_ids), part_ids.numel(), wt, _ptr(weights),
+                                          ctypes.byref(out), ctypes.c_void_p(s))
+    _check(rc)
+    return out.value
 
 
 def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None):

@@ -28,7 +28,8 @@ NVFLAGS = ARCH + [
     "-I" + os.path.join(ROOT, "include"),
 ]
 
-SOURCES = ["engine_core.cu", "inst_ref32.cu", "inst_f64.cu", "inst_band.cu", "split_noalloc.cu", "ffi.cpp"]
+SOURCES = ["engine_core.cu", "inst_ref32.cu", "inst_f64.cu", "inst_band.cu", "split_noalloc.cu", "imbalance.cu",
+           "ffi.cpp"]
 
 
 def _deps_mtime():

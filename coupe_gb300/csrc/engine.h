@@ -59,7 +59,7 @@ constexpr uint64_t TRAV_MAX_ENTRIES = 1ull << 22;
 // Kernel kinds timed by the optional per-launch profiler.
 enum KernelId {
     KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_CHILDREN, KID_REORDER,
-    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_COUNT
+    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_LOADS, KID_COUNT
 };
 const char *kernel_name(int id);
 
@@ -113,6 +113,16 @@ int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
 // The Rib basis change (obb_to_aabb) of n device-resident points.
 int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
                std::string *err);
+
+// Loads of parts 0..P-1 of a device-resident partition (coupe's
+// compute_parts_load), written to the host array `loads` (P elements of the
+// weights' type); COUPE_ERR_BAD_TYPE for a part id >= P or a non-finite
+// f64 weight.
+int parts_load(DevCtx &C, const uint64_t *d_part, uint64_t n, int wtype, const void *d_w, uint64_t P,
+               cudaStream_t stream, void *loads, std::string *err);
+
+// coupe's imbalance from the loads of P parts (host arithmetic).
+double imbalance_of_loads(int wtype, const void *loads, uint64_t P);
 
 // The engine's per-point f64 -> f32 key conversion over n device values.
 int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStream_t stream, std::string *err);

@@ -442,6 +442,147 @@ enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n
     return (coupe_err)rc;
 }
 
+// Loads (and, with `imbalance`, coupe's imbalance of them) of n device part
+// ids and weights; the caller holds C.mu.
+static coupe_err loads_locked(cg::DevCtx &C, const uint64_t *d_part, uint64_t n, int wtype, const void *d_w,
+                              uint64_t num_parts, void *loads, double *imbalance, cudaStream_t s) {
+    if (imbalance && num_parts == 0) {  // imbalance.rs:52-55, before any load is computed
+        *imbalance = 0.0;
+        return COUPE_ERR_OK;
+    }
+    std::vector<uint64_t> tmp;  // 8-byte slots hold any weight type
+    if (imbalance) {
+        tmp.resize(num_parts);
+        loads = tmp.data();
+    }
+    std::string err;
+    const int rc = cg::parts_load(C, d_part, n, wtype, d_w, num_parts, s, loads, &err);
+    if (rc != COUPE_ERR_OK) {
+        t_err = err;
+        return (coupe_err)rc;
+    }
+    if (imbalance) *imbalance = cg::imbalance_of_loads(wtype, loads, num_parts);
+    return COUPE_ERR_OK;
+}
+
+static coupe_err device_loads(const uint64_t *d_partition, uint64_t n, enum coupe_type weight_type,
+                              const void *d_weights, uint64_t num_parts, void *loads, double *imbalance,
+                              void *stream) {
+    t_err.clear();
+    if (imbalance && num_parts == 0) {  // imbalance.rs:52-55, before anything else
+        *imbalance = 0.0;
+        return COUPE_ERR_OK;
+    }
+    if (weight_type < COUPE_INT || weight_type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (!imbalance && num_parts > 0 && !loads) {
+        t_err = "NULL loads";
+        return COUPE_ERR_CRASH;
+    }
+    if (n > 0 && (!d_partition || !d_weights)) {
+        t_err = "NULL partition or weights";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    return loads_locked(*C, d_partition, n, weight_type, d_weights, num_parts, loads, imbalance,
+                        stream ? (cudaStream_t)stream : C->stream);
+}
+
+enum coupe_err coupe_gpu_parts_load_device(const uint64_t *d_partition, uint64_t n, enum coupe_type weight_type,
+                                           const void *d_weights, uint64_t num_parts, void *loads, void *stream) {
+    return device_loads(d_partition, n, weight_type, d_weights, num_parts, loads, nullptr, stream);
+}
+
+enum coupe_err coupe_gpu_imbalance_device(uint64_t num_parts, const uint64_t *d_partition, uint64_t n,
+                                          enum coupe_type weight_type, const void *d_weights, double *imbalance,
+                                          void *stream) {
+    if (!imbalance) {
+        t_err = "NULL imbalance";
+        return COUPE_ERR_CRASH;
+    }
+    return device_loads(d_partition, n, weight_type, d_weights, num_parts, nullptr, imbalance, stream);
+}
+
+// Host forms: the part ids and the weights (gathered like host_call's) are
+// copied to the device, then the loads are computed there.
+static coupe_err host_loads(uintptr_t num_parts, const uintptr_t *partition, const coupe_data *weights, void *loads,
+                            double *imbalance) {
+    t_err.clear();
+    if (!weights) {
+        t_err = "NULL data set";
+        return COUPE_ERR_CRASH;
+    }
+    if (weights->type < COUPE_INT || weights->type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (imbalance && num_parts == 0) {
+        *imbalance = 0.0;
+        return COUPE_ERR_OK;
+    }
+    if (!imbalance && num_parts > 0 && !loads) {
+        t_err = "NULL loads";
+        return COUPE_ERR_CRASH;
+    }
+    const uintptr_t n = weights->len;
+    if (n > 0 && !partition) {
+        t_err = "NULL partition";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    const size_t wsz = type_size(weights->type);
+    const size_t pbytes = (size_t)n * sizeof(uint64_t), wbytes = (size_t)n * wsz;
+    std::lock_guard<std::mutex> lock(C->mu);
+    char *dbuf = (char *)t_dev.get(pbytes + wbytes + 512, C->dev);
+    if (!dbuf) {
+        t_err = "device allocation of the input copy failed";
+        return COUPE_ERR_ALLOC;
+    }
+    uint64_t *d_part = (uint64_t *)dbuf;
+    char *d_w = dbuf + ((pbytes + 255) & ~(size_t)255);
+    static thread_local Staging st_w;
+    const void *src_w = weights->ptr;
+    if (weights->kind != 0 && n > 0) {
+        char *h = (char *)st_w.get(wbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(weights, i, wsz, h + i * wsz);
+        src_w = h;
+    }
+    cudaStream_t s = C->stream;
+    cudaError_t e;
+    if (n > 0 && ((e = cudaMemcpyAsync(d_part, partition, pbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+                  (e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess))
+        return (coupe_err)cg::cuda_fail(e, "host to device copy", &t_err);
+    return loads_locked(*C, d_part, n, weights->type, d_w, num_parts, loads, imbalance, s);
+}
+
+enum coupe_err coupe_gpu_parts_load(const uintptr_t *partition, uintptr_t num_parts, const coupe_data *weights,
+                                    void *loads) {
+    return host_loads(num_parts, partition, weights, loads, nullptr);
+}
+
+enum coupe_err coupe_gpu_imbalance(uintptr_t num_parts, const uintptr_t *partition, const coupe_data *weights,
+                                   double *imbalance) {
+    if (!imbalance) {
+        t_err = "NULL imbalance";
+        return COUPE_ERR_CRASH;
+    }
+    return host_loads(num_parts, partition, weights, nullptr, imbalance);
+}
+
 void coupe_gpu_last_stats(struct coupe_gpu_stats *out) {
     if (out) *out = t_stats;
 }

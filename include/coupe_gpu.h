@@ -105,6 +105,34 @@ enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double
  * The engine computes it with integer instructions. */
 enum coupe_err coupe_gpu_f64_to_f32(const double *d_in, float *d_out, uint64_t n, void *stream);
 
+/* Load of each part of a partition: loads[p] is the sum of the weights of
+ * the points i with partition[i] == p, for p < num_parts
+ * (coupe::imbalance::compute_parts_load, coupe/src/imbalance.rs:14-39).
+ * `loads` (host) receives num_parts elements of the weights' type: c_int
+ * and int64 loads wrap around like coupe's release build; double loads are
+ * the exact sums (128-bit fixed point) rounded once.  Errors:
+ * COUPE_ERR_BAD_TYPE for a part id >= num_parts (coupe panics) or a
+ * non-finite double weight. */
+enum coupe_err coupe_gpu_parts_load(const uintptr_t *partition, uintptr_t num_parts,
+		const coupe_data *weights, void *loads);
+
+/* coupe::imbalance::imbalance (coupe/src/imbalance.rs:41-77): the largest
+ * (load - ideal) / ideal over the parts, ideal = total weight / num_parts;
+ * 0 when num_parts is 0 or the ideal load is 0.  `partition` holds
+ * weights->len part ids.  Errors as coupe_gpu_parts_load. */
+enum coupe_err coupe_gpu_imbalance(uintptr_t num_parts, const uintptr_t *partition,
+		const coupe_data *weights, double *imbalance);
+
+/* Device-resident forms: n part ids in `d_partition`, n weights of
+ * `weight_type` in `d_weights`; `loads` and `imbalance` are host memory.
+ * Return after the work on `stream` completed. */
+enum coupe_err coupe_gpu_parts_load_device(const uint64_t *d_partition, uint64_t n,
+		enum coupe_type weight_type, const void *d_weights, uint64_t num_parts, void *loads,
+		void *stream);
+enum coupe_err coupe_gpu_imbalance_device(uint64_t num_parts, const uint64_t *d_partition,
+		uint64_t n, enum coupe_type weight_type, const void *d_weights, double *imbalance,
+		void *stream);
+
 /* Stable split of one part of device-resident points by a cut, allocating
  * nothing.  No counterpart in the reference: coupe moves the points of a part
  * with an in-place, unstable partition inside Rcb

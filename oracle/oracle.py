@@ -195,3 +195,51 @@ def reorder_split_f32(keys, pivot_index):
     k = np.ascontiguousarray(np.asarray(keys, dtype=np.float32)).copy()
     nl = lib().oracle_reorder_split_f32(k.ctypes.data, len(k), pivot_index)
     return k[:nl], k[nl:]
+
+
+# ---------------------------------------------------------------------------
+# coupe::imbalance (coupe/src/imbalance.rs), restated on the host.
+# ---------------------------------------------------------------------------
+def parts_load(partition, num_parts, weights):
+    """compute_parts_load (imbalance.rs:14-39): the sum of the weights of
+    each part.  Integer loads wrap around in the weights' type (coupe's
+    release build); f64 loads are this oracle's fixed-point sums (one scale
+    for all n weights, fixed_scale / fixed_sum), the order-independent form
+    the GPU computes.  A part id >= num_parts raises IndexError (coupe's
+    `acc[part]` panics)."""
+    ids = np.asarray(partition, dtype=np.uint64)
+    w = np.asarray(weights)
+    if len(ids) != len(w):
+        raise ValueError("partition and weights differ in length")
+    if len(ids) and int(ids.max()) >= num_parts:
+        raise IndexError("part id out of range")
+    if w.dtype == np.float64:
+        s = fixed_scale(w)
+        order = np.argsort(ids, kind="stable")
+        ws = w[order]
+        bounds = np.searchsorted(ids[order], np.arange(num_parts + 1, dtype=np.uint64))
+        return np.array([fixed_sum(ws[bounds[p]:bounds[p + 1]], s) for p in range(num_parts)], dtype=np.float64)
+    acc = np.zeros(num_parts, dtype=np.int64)
+    np.add.at(acc, ids.astype(np.int64), w.astype(np.int64))  # wraps mod 2^64
+    return acc.astype(w.dtype) if w.dtype == np.int32 else acc
+
+
+def imbalance(num_parts, partition, weights):
+    """imbalance (imbalance.rs:41-77): 0 without parts (before any load is
+    computed); else the total load summed in the weights' type, the ideal
+    total / num_parts in f64, 0 when that is 0, and the largest
+    (load - ideal) / ideal."""
+    if num_parts == 0:
+        return 0.0
+    loads = parts_load(partition, num_parts, weights)
+    if loads.dtype == np.float64:
+        total = 0.0
+        for v in loads:
+            total += float(v)
+    else:
+        with np.errstate(over="ignore"):
+            total = float(np.sum(loads, dtype=loads.dtype))
+    ideal = total / float(num_parts)
+    if ideal == 0.0:
+        return 0.0
+    return max((float(v) - ideal) / ideal for v in loads)
