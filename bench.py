@@ -318,6 +318,30 @@ def main():
     imbalance = {"value": imb, "parts": P, "ms_per_call": round(t_imb, 4), "kernel_us": round(1e3 * k_ms, 1),
                  "kernel_GBps": round(kl["bytes"] / max(1, kl["launches"]) / (k_ms / 1e3) / 1e9, 1) if k_ms else None}
 
+    # mesh-part's points: barycentres of a structured 160^3 hexahedral mesh
+    # (4.1M elements, 262 MB of node lists), device-resident, one pass
+    m = 160
+    g = np.arange(m + 1, dtype=np.int64)
+    idx = (g[:, None, None] * (m + 1) + g[None, :, None]) * (m + 1) + g[None, None, :]
+    corners = [idx[:-1, :-1, :-1], idx[1:, :-1, :-1], idx[1:, 1:, :-1], idx[:-1, 1:, :-1],
+               idx[:-1, :-1, 1:], idx[1:, :-1, 1:], idx[1:, 1:, 1:], idx[:-1, 1:, 1:]]
+    d_nodes = torch.from_numpy(np.stack([c.reshape(-1) for c in corners], -1)).to(dev)
+    d_coords = torch.stack(torch.meshgrid(*(torch.arange(m + 1, dtype=torch.float64, device=dev),) * 3,
+                                          indexing="ij"), -1).reshape(-1, 3).contiguous()
+    for _ in range(args.warmup):
+        coupe.barycentres_device(d_coords, d_nodes)
+    barrier()
+    coupe.profile(True)
+    for _ in range(args.steps):
+        coupe.barycentres_device(d_coords, d_nodes)
+    torch.cuda.synchronize()
+    kb = coupe.profile_read().get("k_barycentres", {"ms": 0.0, "bytes": 0, "launches": 1})
+    coupe.profile(False)
+    b_ms = kb["ms"] / max(1, kb["launches"])
+    bary = {"elements": int(d_nodes.shape[0]), "nodes_per_element": 8, "kernel_us": round(1e3 * b_ms, 1),
+            "kernel_GBps": round(kb["bytes"] / max(1, kb["launches"]) / (b_ms / 1e3) / 1e9, 1) if b_ms else None}
+    del d_nodes, d_coords
+
     cpu = None
     parity = {}
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -358,6 +382,7 @@ def main():
                                        for m, pr in by_mode.items()}},
         "parity": parity,
         "imbalance": imbalance,
+        "barycentres": bary,
         "clocks": clocks.summary() if clocks else None,
     }
     if "f32key_f64band" in results:

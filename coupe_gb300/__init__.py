@@ -41,6 +41,7 @@ EXPORTED = [
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
     "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
     "coupe_gpu_parts_load", "coupe_gpu_imbalance", "coupe_gpu_parts_load_device", "coupe_gpu_imbalance_device",
+    "coupe_gpu_barycentres",
 ]
 
 
@@ -134,6 +135,8 @@ def lib():
     L.coupe_gpu_parts_load_device.restype = i32
     L.coupe_gpu_imbalance_device.argtypes = [u64, vp, u64, i32, vp, ctypes.POINTER(dbl), vp]
     L.coupe_gpu_imbalance_device.restype = i32
+    L.coupe_gpu_barycentres.argtypes = [u64, u64, vp, u64, u64, vp, vp, vp]
+    L.coupe_gpu_barycentres.restype = i32
     L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     L.coupe_gpu_set_option.restype = i32
     L.coupe_gpu_get_option.argtypes = [ctypes.c_char_p]
@@ -417,6 +420,32 @@ def imbalance_device(num_parts, part_ids, weights, stream=None):
                                           ctypes.byref(out), ctypes.c_void_p(s))
     _check(rc)
     return out.value
+
+
+def barycentres_device(coords, nodes, stream=None):
+    """Element barycentres on CUDA tensors (mesh-part's points,
+    tools/lib/lib.rs:511-539): coords float64 (n_nodes, D), nodes int64 or
+    uint64 (n_elements, k) 0-based; returns a float64 (n_elements, D) tensor.
+    Bit-identical to coupe's sums in node order divided by k."""
+    import torch
+    n_nodes, dim = coords.shape
+    n_el, k = nodes.shape
+    out = torch.empty((n_el, dim), dtype=torch.float64, device=coords.device)
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_barycentres(dim, n_nodes, _ptr(coords), n_el, k, _ptr(nodes), _ptr(out), ctypes.c_void_p(s))
+    _check(rc)
+    return out
+
+
+def barycentres_host(coords, nodes):
+    """barycentres_device on host arrays (uploaded, computed on the GPU,
+    read back)."""
+    import torch
+    c = torch.from_numpy(np.ascontiguousarray(coords, dtype=np.float64)).cuda()
+    v = torch.from_numpy(np.ascontiguousarray(np.asarray(nodes).astype(np.int64, copy=False))).cuda()
+    if v.dim() != 2 or v.shape[0] == 0:
+        return np.zeros((0 if v.dim() != 2 else v.shape[0], c.shape[1]))
+    return barycentres_device(c, v).cpu().numpy()
 
 
 def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None):

@@ -59,7 +59,7 @@ constexpr uint64_t TRAV_MAX_ENTRIES = 1ull << 22;
 // Kernel kinds timed by the optional per-launch profiler.
 enum KernelId {
     KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_CHILDREN, KID_REORDER,
-    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_LOADS, KID_COUNT
+    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_LOADS, KID_BARY, KID_COUNT
 };
 const char *kernel_name(int id);
 
@@ -123,6 +123,11 @@ int parts_load(DevCtx &C, const uint64_t *d_part, uint64_t n, int wtype, const v
 
 // coupe's imbalance from the loads of P parts (host arithmetic).
 double imbalance_of_loads(int wtype, const void *loads, uint64_t P);
+
+// Barycentres of n_el elements of k nodes each (device node lists, 0-based)
+// over n_nodes device coordinates of `dim` doubles; d_out gets n_el x dim.
+int barycentres(DevCtx &C, int dim, const double *d_coords, uint64_t n_nodes, uint64_t k, const uint64_t *d_nodes,
+                uint64_t n_el, double *d_out, cudaStream_t stream, std::string *err);
 
 // The engine's per-point f64 -> f32 key conversion over n device values.
 int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStream_t stream, std::string *err);

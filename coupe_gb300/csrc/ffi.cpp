@@ -569,6 +569,33 @@ static coupe_err host_loads(uintptr_t num_parts, const uintptr_t *partition, con
     return loads_locked(*C, d_part, n, weights->type, d_w, num_parts, loads, imbalance, s);
 }
 
+enum coupe_err coupe_gpu_barycentres(uint64_t dimension, uint64_t n_nodes, const double *d_coords,
+                                     uint64_t n_elements, uint64_t nodes_per_element, const uint64_t *d_nodes,
+                                     double *d_out, void *stream) {
+    t_err.clear();
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (nodes_per_element != 2 && nodes_per_element != 3 && nodes_per_element != 4 && nodes_per_element != 8) {
+        t_err = "elements of 2, 3, 4 or 8 nodes";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (n_elements == 0) return COUPE_ERR_OK;
+    if (!d_coords || !d_nodes || !d_out) {
+        t_err = "NULL array";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    const int rc = cg::barycentres(*C, (int)dimension, d_coords, n_nodes, nodes_per_element, d_nodes, n_elements,
+                                   d_out, (cudaStream_t)stream, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
 enum coupe_err coupe_gpu_parts_load(const uintptr_t *partition, uintptr_t num_parts, const coupe_data *weights,
                                     void *loads) {
     return host_loads(num_parts, partition, weights, loads, nullptr);

@@ -123,6 +123,20 @@ enum coupe_err coupe_gpu_parts_load(const uintptr_t *partition, uintptr_t num_pa
 enum coupe_err coupe_gpu_imbalance(uintptr_t num_parts, const uintptr_t *partition,
 		const coupe_data *weights, double *imbalance);
 
+/* Barycentres of one block of mesh elements with the same node count
+ * (mesh-part's points, tools/lib/lib.rs:511-539): element e's point is the
+ * sum of the coordinates of its nodes d_nodes[e * nodes_per_element + j]
+ * (0-based, in that order, from 0.0) divided by nodes_per_element.
+ * Device arrays: d_coords (n_nodes x dimension doubles), d_nodes
+ * (n_elements x nodes_per_element), d_out (n_elements x dimension).
+ * dimension 2 or 3 (else COUPE_ERR_BAD_DIMENSION); nodes_per_element 2, 3,
+ * 4 or 8 (else COUPE_ERR_BAD_TYPE); a node index >= n_nodes returns
+ * COUPE_ERR_BAD_TYPE (coupe panics).  Returns after the work on `stream`
+ * completed. */
+enum coupe_err coupe_gpu_barycentres(uint64_t dimension, uint64_t n_nodes, const double *d_coords,
+		uint64_t n_elements, uint64_t nodes_per_element, const uint64_t *d_nodes, double *d_out,
+		void *stream);
+
 /* Device-resident forms: n part ids in `d_partition`, n weights of
  * `weight_type` in `d_weights`; `loads` and `imbalance` are host memory.
  * Return after the work on `stream` completed. */

@@ -243,3 +243,15 @@ def imbalance(num_parts, partition, weights):
     if ideal == 0.0:
         return 0.0
     return max((float(v) - ideal) / ideal for v in loads)
+
+
+def barycentres(coords, nodes):
+    """mesh-part's points (tools/lib/lib.rs:511-539) for one element block:
+    per element, 0.0 plus its node coordinates in node order, divided by the
+    node count."""
+    c = np.asarray(coords, dtype=np.float64)
+    v = np.asarray(nodes, dtype=np.int64)
+    acc = np.zeros((len(v), c.shape[1]))
+    for j in range(v.shape[1]):
+        acc = acc + c[v[:, j]]
+    return acc / float(v.shape[1])
