@@ -342,6 +342,24 @@ def main():
             "kernel_GBps": round(kb["bytes"] / max(1, kb["launches"]) / (b_ms / 1e3) / 1e9, 1) if b_ms else None}
     del d_nodes, d_coords
 
+    # coupe's Grid::rcb: a 256^3 grid of int64 weights U{1..99} in 1024
+    # parts, medians replaying 16 rayon workers
+    gsz = (256, 256, 256)
+    gn = 256 ** 3
+    g_w = torch.from_numpy(np.random.default_rng(3).integers(1, 100, gn)).to(dev)
+    g_ids = torch.zeros(gn, dtype=torch.int64, device=dev)
+    for _ in range(args.warmup):
+        coupe.grid_rcb_device(g_ids, g_w, gsz, 10, 16)
+    barrier()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        coupe.grid_rcb_device(g_ids, g_w, gsz, 10, 16)
+    ev1.record(stream)
+    barrier()
+    grid = {"cells": gn, "parts": 1024, "threads_replayed": 16,
+            "ms_per_call": round(ev0.elapsed_time(ev1) / args.steps, 3)}
+    del g_w, g_ids
+
     cpu = None
     parity = {}
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -383,6 +401,7 @@ def main():
         "parity": parity,
         "imbalance": imbalance,
         "barycentres": bary,
+        "grid_rcb": grid,
         "clocks": clocks.summary() if clocks else None,
     }
     if "f32key_f64band" in results:

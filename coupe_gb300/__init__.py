@@ -41,7 +41,7 @@ EXPORTED = [
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
     "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
     "coupe_gpu_parts_load", "coupe_gpu_imbalance", "coupe_gpu_parts_load_device", "coupe_gpu_imbalance_device",
-    "coupe_gpu_barycentres",
+    "coupe_gpu_barycentres", "coupe_gpu_grid_rcb", "coupe_gpu_grid_rcb_device",
 ]
 
 
@@ -135,6 +135,10 @@ def lib():
     L.coupe_gpu_parts_load_device.restype = i32
     L.coupe_gpu_imbalance_device.argtypes = [u64, vp, u64, i32, vp, ctypes.POINTER(dbl), vp]
     L.coupe_gpu_imbalance_device.restype = i32
+    L.coupe_gpu_grid_rcb.argtypes = [vp, u64, vp, vp, u64, u64]
+    L.coupe_gpu_grid_rcb.restype = i32
+    L.coupe_gpu_grid_rcb_device.argtypes = [vp, u64, vp, i32, vp, u64, u64, vp]
+    L.coupe_gpu_grid_rcb_device.restype = i32
     L.coupe_gpu_barycentres.argtypes = [u64, u64, vp, u64, u64, vp, vp, vp]
     L.coupe_gpu_barycentres.restype = i32
     L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
@@ -420,6 +424,62 @@ def imbalance_device(num_parts, part_ids, weights, stream=None):
                                           ctypes.byref(out), ctypes.c_void_p(s))
     _check(rc)
     return out.value
+
+
+class Grid:
+    """A 2D or 3D cartesian grid (coupe::Grid, coupe/src/cartesian/mod.rs):
+    cell (x, y[, z]) is entry x + size[0] * (y + size[1] * z) of the weights
+    and of the partition."""
+
+    def __init__(self, *size):
+        if len(size) == 1 and not np.isscalar(size[0]):
+            size = tuple(size[0])
+        self.size = tuple(int(v) for v in size)
+
+    @classmethod
+    def new_2d(cls, width, height):
+        return cls(width, height)
+
+    @classmethod
+    def new_3d(cls, width, height, depth):
+        return cls(width, height, depth)
+
+    def __len__(self):
+        return int(np.prod(self.size))
+
+    def rcb(self, partition, weights, iter_count, threads=None):
+        """Grid::rcb through coupe_gpu_grid_rcb: writes ids in
+        [0, 2**iter_count) into `partition` (uint64, one per cell).  The
+        weighted median replays `threads` rayon workers (default: the host's
+        CPU count, what a default rayon pool uses; at least 2)."""
+        if threads is None:
+            threads = max(2, os.cpu_count() or 2)
+        w = _as_weights(weights, len(self))
+        if partition.dtype != np.uint64 or not partition.flags.c_contiguous:
+            raise TypeError("partition must be a contiguous uint64 array")
+        if len(partition) != len(w):
+            raise CoupeError(ERR_LEN_MISMATCH)
+        sz = np.ascontiguousarray(np.asarray(self.size, dtype=np.uint64))
+        L = lib()
+        dw = L.coupe_data_array(len(w), _weight_type(w), w.ctypes.data)
+        try:
+            rc = L.coupe_gpu_grid_rcb(partition.ctypes.data, len(self.size), sz.ctypes.data, dw, iter_count,
+                                      int(threads))
+        finally:
+            L.coupe_data_free(dw)
+        _check(rc)
+
+
+def grid_rcb_device(part_ids, weights, size, iter_count, threads, stream=None):
+    """Grid::rcb on CUDA tensors: part_ids int64/uint64 and weights
+    int32/int64/float64, one per cell of the grid `size`."""
+    import torch
+    wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+    sz = np.ascontiguousarray(np.asarray(size, dtype=np.uint64))
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_grid_rcb_device(_ptr(part_ids), len(sz), sz.ctypes.data, wt, _ptr(weights), iter_count,
+                                         int(threads), ctypes.c_void_p(s))
+    _check(rc)
 
 
 def barycentres_device(coords, nodes, stream=None):

@@ -59,7 +59,7 @@ constexpr uint64_t TRAV_MAX_ENTRIES = 1ull << 22;
 // Kernel kinds timed by the optional per-launch profiler.
 enum KernelId {
     KID_CONVERT, KID_WABS, KID_WSUM, KID_ROOT, KID_HIST, KID_DECIDE, KID_CHILDREN, KID_REORDER,
-    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_LOADS, KID_BARY, KID_COUNT
+    KID_ASSIGN, KID_FILL, KID_MOMENTS, KID_LOADS, KID_BARY, KID_GRID, KID_COUNT
 };
 const char *kernel_name(int id);
 
@@ -123,6 +123,12 @@ int parts_load(DevCtx &C, const uint64_t *d_part, uint64_t n, int wtype, const v
 
 // coupe's imbalance from the loads of P parts (host arithmetic).
 double imbalance_of_loads(int wtype, const void *loads, uint64_t P);
+
+// coupe's Grid::rcb on a device-resident grid of `dim` sizes (cells
+// x + size[0] * (y + size[1] * z)); the weighted median replays `threads`
+// rayon workers (>= 2).
+int grid_rcb(DevCtx &C, int dim, const uint64_t *size, int wtype, const void *d_w, uint64_t iters, uint64_t threads,
+             uint64_t *d_part, cudaStream_t stream, std::string *err);
 
 // Barycentres of n_el elements of k nodes each (device node lists, 0-based)
 // over n_nodes device coordinates of `dim` doubles; d_out gets n_el x dim.

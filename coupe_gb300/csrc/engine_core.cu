@@ -20,7 +20,7 @@ const char *kernel_name(int id) {
     // KID_ASSIGN: the kernel writing the part ids (a traversal, or k_assign)
     static const char *names[KID_COUNT] = {"k_convert", "k_wabs_max", "k_wsum", "k_root", "k_hist", "k_decide",
                                            "k_children", "k_reorder", "k_ids", "k_fill_u64", "k_moments",
-                                           "k_part_loads", "k_barycentres"};
+                                           "k_part_loads", "k_barycentres", "k_grid"};
     return id >= 0 && id < KID_COUNT ? names[id] : "?";
 }
 

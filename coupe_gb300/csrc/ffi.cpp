@@ -569,6 +569,120 @@ static coupe_err host_loads(uintptr_t num_parts, const uintptr_t *partition, con
     return loads_locked(*C, d_part, n, weights->type, d_w, num_parts, loads, imbalance, s);
 }
 
+// Argument checks of Grid::rcb shared by both entry points.
+static coupe_err grid_checks(uint64_t dimension, const uint64_t *size, uint64_t n_weights, uint64_t threads,
+                             uint64_t *cells) {
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (!size) {
+        t_err = "NULL size";
+        return COUPE_ERR_CRASH;
+    }
+    uint64_t n = 1;
+    for (uint64_t d = 0; d < dimension; ++d) {
+        if (size[d] == 0) return COUPE_ERR_BAD_DIMENSION;  // coupe's sizes are NonZeroUsize
+        if (n > UINT64_MAX / size[d]) {
+            t_err = "grid too large";
+            return COUPE_ERR_ALLOC;
+        }
+        n *= size[d];
+    }
+    if (n_weights != n) return COUPE_ERR_LEN_MISMATCH;
+    if (threads < 2) {
+        t_err = "threads must be at least 2 (coupe's median search does not end with one worker)";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    *cells = n;
+    return COUPE_ERR_OK;
+}
+
+enum coupe_err coupe_gpu_grid_rcb_device(uint64_t *d_partition, uint64_t dimension, const uint64_t *size,
+                                         enum coupe_type weight_type, const void *d_weights, uint64_t iter_count,
+                                         uint64_t threads, void *stream) {
+    t_err.clear();
+    if (weight_type < COUPE_INT || weight_type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    uint64_t n = 0, nw = 1;
+    if (size && (dimension == 2 || dimension == 3))
+        for (uint64_t d = 0; d < dimension; ++d) nw *= size[d];
+    const coupe_err c = grid_checks(dimension, size, nw, threads, &n);
+    if (c != COUPE_ERR_OK) return c;
+    if (!d_partition || !d_weights) {
+        t_err = "NULL partition or weights";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    const int rc = cg::grid_rcb(*C, (int)dimension, size, weight_type, d_weights, iter_count, threads, d_partition,
+                                (cudaStream_t)stream, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+enum coupe_err coupe_gpu_grid_rcb(uintptr_t *partition, uintptr_t dimension, const uintptr_t *size,
+                                  const coupe_data *weights, uintptr_t iter_count, uintptr_t threads) {
+    t_err.clear();
+    if (!weights) {
+        t_err = "NULL data set";
+        return COUPE_ERR_CRASH;
+    }
+    if (weights->type < COUPE_INT || weights->type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    static_assert(sizeof(uintptr_t) == sizeof(uint64_t), "64-bit uintptr_t expected");
+    uint64_t n = 0;
+    const coupe_err c = grid_checks(dimension, (const uint64_t *)size, weights->len, threads, &n);
+    if (c != COUPE_ERR_OK) return c;
+    if (!partition) {
+        t_err = "NULL partition";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    const size_t wsz = type_size(weights->type), wbytes = (size_t)n * wsz, obytes = (size_t)n * 8;
+    std::lock_guard<std::mutex> lock(C->mu);
+    char *dbuf = (char *)t_dev.get(wbytes + obytes + 512, C->dev);
+    if (!dbuf) {
+        t_err = "device allocation of the input copy failed";
+        return COUPE_ERR_ALLOC;
+    }
+    char *d_w = dbuf;
+    uint64_t *d_part = (uint64_t *)(dbuf + ((wbytes + 255) & ~(size_t)255));
+    static thread_local Staging st_w;
+    const void *src_w = weights->ptr;
+    if (weights->kind != 0) {
+        char *h = (char *)st_w.get(wbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(weights, i, wsz, h + i * wsz);
+        src_w = h;
+    }
+    cudaStream_t s = C->stream;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "host to device copy", &t_err);
+    const int rc = cg::grid_rcb(*C, (int)dimension, (const uint64_t *)size, weights->type, d_w, iter_count, threads,
+                                d_part, s, &err);
+    if (rc != COUPE_ERR_OK) {
+        t_err = err;
+        return (coupe_err)rc;
+    }
+    if ((e = cudaMemcpyAsync(partition, d_part, obytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "device to host copy", &t_err);
+    return COUPE_ERR_OK;
+}
+
 enum coupe_err coupe_gpu_barycentres(uint64_t dimension, uint64_t n_nodes, const double *d_coords,
                                      uint64_t n_elements, uint64_t nodes_per_element, const uint64_t *d_nodes,
                                      double *d_out, void *stream) {

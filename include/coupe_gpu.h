@@ -123,6 +123,26 @@ enum coupe_err coupe_gpu_parts_load(const uintptr_t *partition, uintptr_t num_pa
 enum coupe_err coupe_gpu_imbalance(uintptr_t num_parts, const uintptr_t *partition,
 		const coupe_data *weights, double *imbalance);
 
+/* Rcb on a cartesian grid (coupe::Grid::rcb, coupe/src/cartesian/mod.rs:
+ * 130-179, cartesian/rcb.rs:52-281): `size` holds `dimension` (2 or 3) cell
+ * counts; cell (x, y[, z]) is weight and partition entry
+ * x + size[0] * (y + size[1] * z).  Splits start on axis 1 and cycle; each
+ * is coupe's weighted median of the slab weights, which replays rayon's
+ * fold_chunks with `threads` workers: pass the size of the rayon pool whose
+ * result is to be reproduced (>= 2; with one worker coupe's search never
+ * ends, and COUPE_ERR_BAD_TYPE is returned).  Ids are in
+ * [0, 2^iter_count).  Integer weights wrap like coupe's release build; the
+ * total of double weights is their exact sum rounded once (coupe's rayon
+ * sum has no fixed order).  Errors: COUPE_ERR_BAD_DIMENSION for a dimension
+ * other than 2 or 3 or a zero size, COUPE_ERR_LEN_MISMATCH unless the
+ * weights hold one value per cell, COUPE_ERR_BAD_TYPE for a non-finite
+ * double weight. */
+enum coupe_err coupe_gpu_grid_rcb(uintptr_t *partition, uintptr_t dimension, const uintptr_t *size,
+		const coupe_data *weights, uintptr_t iter_count, uintptr_t threads);
+enum coupe_err coupe_gpu_grid_rcb_device(uint64_t *d_partition, uint64_t dimension, const uint64_t *size,
+		enum coupe_type weight_type, const void *d_weights, uint64_t iter_count, uint64_t threads,
+		void *stream);
+
 /* Barycentres of one block of mesh elements with the same node count
  * (mesh-part's points, tools/lib/lib.rs:511-539): element e's point is the
  * sum of the coordinates of its nodes d_nodes[e * nodes_per_element + j]

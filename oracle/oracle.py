@@ -255,3 +255,150 @@ def barycentres(coords, nodes):
     for j in range(v.shape[1]):
         acc = acc + c[v[:, j]]
     return acc / float(v.shape[1])
+
+
+# ---------------------------------------------------------------------------
+# coupe::Grid::rcb (coupe/src/cartesian/mod.rs:130-179, cartesian/rcb.rs:52-281)
+# restated on the host.  The weighted median replays rayon's fold_chunks with
+# `threads` workers (cartesian/rcb.rs:67-72), so the split positions depend
+# on that count exactly as coupe's do.  The root's f64 total is the
+# fixed-point sum rounded once (coupe's rayon sum has no fixed order).
+# ---------------------------------------------------------------------------
+GRID_TOLERANCE = 0.01  # cartesian/rcb.rs:45
+
+_INT_RANGE = {np.dtype(np.int32): (-(2**31), 2**31 - 1), np.dtype(np.int64): (-(2**63), 2**63 - 1)}
+
+
+def _w_from_f64(x, dt):
+    """f64 `as` W: truncation toward zero, saturating, NaN -> 0."""
+    if dt == np.float64:
+        return float(x)
+    if x != x:
+        return 0
+    lo, hi = _INT_RANGE[dt]
+    if x >= hi:
+        return hi
+    if x <= lo:
+        return lo
+    return int(x)
+
+
+def _w_wrap(v, dt):
+    if dt == np.float64:
+        return float(v)
+    bits = 32 if dt == np.int32 else 64
+    v &= (1 << bits) - 1
+    return v - (1 << bits) if v >> (bits - 1) else v
+
+
+def grid_weighted_median(weights, total, threads, dt):
+    """weighted_median (cartesian/rcb.rs:53-101): (position, left weight).
+    threads >= 2 (with one worker coupe's loop does not end)."""
+    dt = np.dtype(dt)
+    ideal = float(total) / 2.0
+    min_part = _w_from_f64(ideal * (1.0 - GRID_TOLERANCE), dt)
+    max_part = _w_from_f64(ideal * (1.0 + GRID_TOLERANCE), dt)
+    zero = 0.0 if dt == np.float64 else 0
+    w = [float(x) if dt == np.float64 else int(x) for x in weights]
+    lo, hi, left = 0, len(w), zero
+    while True:
+        cs = max(1, (hi - lo) // threads)
+        left0, prefix = left, zero
+        for start in range(lo, hi, cs):
+            pcw = _w_wrap(left0 + prefix, dt)
+            csum = zero
+            for x in w[start:min(start + cs, hi)]:
+                csum = _w_wrap(csum + x, dt)
+            prefix = _w_wrap(prefix + csum, dt)
+            if pcw < min_part:
+                lo, left = start, pcw
+            elif max_part < pcw:
+                hi = start
+                break
+            else:
+                return start, pcw
+        if lo + 1 >= hi:
+            return lo, left
+
+
+def _grid_axis_sums(w, off, sz, coord, dt):
+    """The sums of the subgrid's slabs along `coord`, each in coupe's order
+    (cartesian/rcb.rs:119-141, 192-238): 2D w[y, x]; 3D w[z, y, x]."""
+    D = w.ndim
+    out = []
+    rng = [range(off[d], off[d] + sz[d]) for d in range(D)]
+    for p in rng[coord]:
+        if D == 2:
+            x0, x1, y0, y1 = off[0], off[0] + sz[0], off[1], off[1] + sz[1]
+            slab = w[y0:y1, p] if coord == 0 else w[p, x0:x1]
+        else:
+            x0, x1, y0, y1, z0, z1 = (off[0], off[0] + sz[0], off[1], off[1] + sz[1], off[2], off[2] + sz[2])
+            if coord == 0:
+                slab = w[z0:z1, y0:y1, p].T  # y outer, z inner
+            elif coord == 1:
+                slab = w[z0:z1, p, x0:x1]  # z outer, x inner
+            else:
+                slab = w[p, y0:y1, x0:x1].T  # x outer, y inner
+        flat = np.ascontiguousarray(slab).reshape(-1)
+        if dt == np.float64:
+            out.append(float(np.cumsum(flat)[-1]) if len(flat) else 0.0)
+        else:
+            out.append(_w_wrap(int(flat.astype(np.int64).sum(dtype=np.int64)), dt))
+    return out
+
+
+def grid_rcb(size, weights, iter_count, threads):
+    """Grid::rcb (cartesian/mod.rs:130-179): part ids of the cells (index
+    x + width * (y + height * z)), in [0, 2^iter_count)."""
+    D = len(size)
+    wv = np.asarray(weights)
+    dt = wv.dtype
+    w = wv.reshape(tuple(reversed(size)))
+    if dt == np.float64:
+        total = fixed_sum(wv, fixed_scale(wv)) if len(wv) else 0.0
+    else:
+        total = _w_wrap(int(wv.astype(np.int64).sum(dtype=np.int64)), dt)
+    tree = {}
+
+    def rec(node, off, sz, tot, iters, coord):
+        if sz[coord] == 0 or iters == 0:
+            tree[node] = None
+            return
+        axis = _grid_axis_sums(w, off, sz, coord, dt)
+        pos, left = grid_weighted_median(axis, tot, threads, dt)
+        at = pos + off[coord]
+        right = _w_wrap(tot - left, dt)
+        lo_sz, hi_sz, hi_off = list(sz), list(sz), list(off)
+        lo_sz[coord] = at - off[coord]
+        hi_sz[coord] -= at - off[coord]
+        hi_off[coord] = at
+        tree[node] = at
+        nxt = (coord + 1) % D
+        rec(2 * node + 1, off, lo_sz, left, iters - 1, nxt)
+        rec(2 * node + 2, hi_off, hi_sz, right, iters - 1, nxt)
+
+    rec(0, [0] * D, list(size), total, iter_count, 1)
+    n = int(np.prod(size))
+    idx = np.arange(n)
+    pos = [idx % size[0], (idx // size[0]) % size[1]] + ([idx // size[0] // size[1]] if D == 3 else [])
+    ids = np.zeros(n, dtype=np.uint64)
+    node = np.zeros(n, dtype=np.int64)
+    coord = 1
+    active = np.ones(n, dtype=bool)
+    while active.any():
+        nxt_node = node.copy()
+        for nd in np.unique(node[active]):
+            at = tree.get(int(nd))
+            m = active & (node == nd)
+            if at is None:
+                active &= ~m
+                continue
+            right = m & (pos[coord] >= at)
+            left = m & ~right
+            ids[left] = ids[left] * 2
+            ids[right] = ids[right] * 2 + 1
+            nxt_node[left] = 2 * nd + 1
+            nxt_node[right] = 2 * nd + 2
+        node = nxt_node
+        coord = (coord + 1) % D
+    return ids
