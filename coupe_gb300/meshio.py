@@ -105,12 +105,15 @@ def _int(word, lineno, signed=False):
     body = word[1:] if word[:1] in "+-" else word
     if not body.isdigit() or not body.isascii() or (word[:1] == "-" and not signed):
         raise MeshIoError("bad_integer", "when parsing integer: %r" % word, lineno)
-    return int(word, 10)
+    v = int(word, 10)
+    if not (-(2**63) <= v < 2**63 if signed else v < 2**64):
+        raise MeshIoError("bad_integer", "when parsing integer: %r (out of range)" % word, lineno)
+    return v
 
 
 def _float(word, lineno):
     try:
-        if "_" in word:
+        if "_" in word or not word.isascii():
             raise ValueError
         return float(word)
     except ValueError:
