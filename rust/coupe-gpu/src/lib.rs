@@ -37,6 +37,12 @@ unsafe extern "C" {
                      weights: *const CoupeData, iter_count: usize, tolerance: f64, mode: c_int) -> c_int;
     fn coupe_gpu_rib(partition: *mut usize, dimension: usize, points: *const CoupeData,
                      weights: *const CoupeData, iter_count: usize, tolerance: f64, mode: c_int) -> c_int;
+    fn coupe_gpu_parts_load(partition: *const usize, num_parts: usize, weights: *const CoupeData,
+                            loads: *mut c_void) -> c_int;
+    fn coupe_gpu_imbalance(num_parts: usize, partition: *const usize, weights: *const CoupeData,
+                           imbalance: *mut f64) -> c_int;
+    fn coupe_gpu_grid_rcb(partition: *mut usize, dimension: usize, size: *const usize, weights: *const CoupeData,
+                          iter_count: usize, threads: usize) -> c_int;
 }
 
 /// Key precision (enum coupe_gpu_mode).
@@ -47,6 +53,8 @@ pub enum Mode {
     Ref32 = 0,
     /// The same algorithm in f64.
     F64 = 1,
+    /// f32 keys with f64 decisions in the band of each cut: F64's ids.
+    F32KeyF64Band = 2,
 }
 
 /// Weight types the library accepts (enum coupe_type).
@@ -137,5 +145,87 @@ where
                  -> Result<(), coupe::Error> {
         let weights: Vec<W::Item> = weights.into_par_iter().collect();
         run(true, part_ids, points, &weights, self.iter_count, self.tolerance, self.mode)
+    }
+}
+
+/// coupe::imbalance on the GPU (coupe/src/imbalance.rs:14-77).  Integer
+/// loads wrap like coupe's release build; f64 loads are exact sums rounded
+/// once.  A part id >= num_parts panics, as coupe's indexing does.
+pub mod imbalance {
+    use super::*;
+
+    /// The load of each part (see `coupe::imbalance::compute_parts_load`).
+    pub fn compute_parts_load<W: GpuWeight + Default>(partition: &[usize], num_parts: usize, weights: &[W]) -> Vec<W> {
+        assert_eq!(partition.len(), weights.len());
+        let mut loads = vec![W::default(); num_parts];
+        let rc = unsafe {
+            let w = coupe_data_array(weights.len(), W::TYPE, weights.as_ptr() as *const c_void);
+            let rc = coupe_gpu_parts_load(partition.as_ptr(), num_parts, w, loads.as_mut_ptr() as *mut c_void);
+            coupe_data_free(w);
+            rc
+        };
+        assert_eq!(rc, ERR_OK, "libcoupe_gpu error {rc}");
+        loads
+    }
+
+    /// The imbalance of a partition (see `coupe::imbalance::imbalance`).
+    pub fn imbalance<W: GpuWeight>(num_parts: usize, partition: &[usize], weights: &[W]) -> f64 {
+        assert_eq!(partition.len(), weights.len());
+        let mut out = 0.0;
+        let rc = unsafe {
+            let w = coupe_data_array(weights.len(), W::TYPE, weights.as_ptr() as *const c_void);
+            let rc = coupe_gpu_imbalance(num_parts, partition.as_ptr(), w, &mut out);
+            coupe_data_free(w);
+            rc
+        };
+        assert_eq!(rc, ERR_OK, "libcoupe_gpu error {rc}");
+        out
+    }
+}
+
+/// A cartesian grid whose Rcb runs on the GPU (see `coupe::Grid`,
+/// coupe/src/cartesian/mod.rs:130-179).  The weighted median replays the
+/// current rayon pool's worker count, so the ids equal coupe's in the same
+/// process.
+#[derive(Clone, Copy, Debug)]
+pub struct Grid<const D: usize> {
+    size: [usize; D],
+}
+
+impl<const D: usize> Grid<D> {
+    fn run<W: GpuWeight>(self, partition: &mut [usize], weights: &[W], iter_count: usize) {
+        let cells: usize = self.size.iter().product();
+        assert_eq!(partition.len(), cells);
+        let rc = unsafe {
+            let w = coupe_data_array(weights.len(), W::TYPE, weights.as_ptr() as *const c_void);
+            let rc = coupe_gpu_grid_rcb(partition.as_mut_ptr(), D, self.size.as_ptr(), w, iter_count,
+                                        rayon::current_num_threads().max(2));
+            coupe_data_free(w);
+            rc
+        };
+        assert_eq!(rc, ERR_OK, "libcoupe_gpu error {rc}");
+    }
+}
+
+impl Grid<2> {
+    pub fn new_2d(width: std::num::NonZeroUsize, height: std::num::NonZeroUsize) -> Self {
+        Self { size: [width.get(), height.get()] }
+    }
+
+    /// Rcb on the 2D grid (see `coupe::Grid::<2>::rcb`); weights and ids row major.
+    pub fn rcb<W: GpuWeight>(self, partition: &mut [usize], weights: &[W], iter_count: usize) {
+        self.run(partition, weights, iter_count)
+    }
+}
+
+impl Grid<3> {
+    pub fn new_3d(width: std::num::NonZeroUsize, height: std::num::NonZeroUsize,
+                  depth: std::num::NonZeroUsize) -> Self {
+        Self { size: [width.get(), height.get(), depth.get()] }
+    }
+
+    /// Rcb on the 3D grid (see `coupe::Grid::<3>::rcb`).
+    pub fn rcb<W: GpuWeight>(self, partition: &mut [usize], weights: &[W], iter_count: usize) {
+        self.run(partition, weights, iter_count)
     }
 }
