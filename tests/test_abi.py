@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -108,3 +109,30 @@ def test_batched_arguments_checked_before_the_device(coupe):
     assert f(dev, 0, None, 3, dev, coupe.COUPE_INT64, dev, None, 0.1, 0, None) == coupe.ERR_OK
     assert f(dev, 2, empty.ctypes.data, 3, dev, coupe.COUPE_INT64, dev, it.ctypes.data, 0.1, 0, None) == coupe.ERR_OK
     assert f(dev, 2, None, 3, dev, coupe.COUPE_INT64, dev, None, 0.1, 0, None) == coupe.ERR_LEN_MISMATCH
+
+
+def test_headers_compile_as_c_and_cpp(tmp_path):
+    """include/*.h are plain C headers (a C or C++ program can bind them)."""
+    import shutil
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = tmp_path / "h.c"
+    src.write_text('#include "coupe.h"\n#include "coupe_gpu.h"\nint main(void) { return 0; }\n')
+    for cc, args in (("gcc", ["-std=c99", "-pedantic"]), ("g++", ["-std=c++17", "-x", "c++"])):
+        if shutil.which(cc) is None:
+            continue
+        r = subprocess.run([cc, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I", os.path.join(root, "include")]
+                           + args + [str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+def test_python_argument_checks_before_the_device(coupe):
+    """Length checks of the Python mirror raise before any device work."""
+    with pytest.raises(coupe.CoupeError):
+        coupe.compute_parts_load(np.array([0, 1], dtype=np.uint64), 2, np.array([1]))
+    with pytest.raises(coupe.CoupeError):
+        coupe.imbalance(2, np.array([0, 1], dtype=np.uint64), np.array([1, 2, 3]))
+    with pytest.raises(coupe.CoupeError):
+        coupe.Grid(3, 4).rcb(np.zeros(11, dtype=np.uint64), np.ones(12), 2, threads=4)
+    with pytest.raises(coupe.CoupeError):
+        coupe.Grid(3, 4).rcb(np.zeros(12, dtype=np.uint64), np.ones(12), 2, threads=1)
