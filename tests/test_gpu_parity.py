@@ -381,7 +381,7 @@ def test_key_conversion_is_ieee_rne(coupe):
                           0x3690000000000001, 0x380FFFFFE0000000], dtype=np.uint64))
     b = np.concatenate(bits)
     x = b.view(np.float64)
-    with np.errstate(over="ignore"):
+    with np.errstate(over="ignore", invalid="ignore"):
         want = x.astype(np.float32)
     d_in = torch.from_numpy(x.copy()).cuda()
     d_out = torch.empty(len(x), dtype=torch.float32, device="cuda")
