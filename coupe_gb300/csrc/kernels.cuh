@@ -25,7 +25,14 @@ constexpr int BLOCK = 256;
 constexpr int NWARPS = BLOCK / 32;
 constexpr int MAX_NBK = 10;
 constexpr int MAX_NB = 1 << MAX_NBK;
-constexpr int HIST_ITEMS = 8;                // items per thread per hist iteration
+#ifndef CG_HIST_ITEMS
+#define CG_HIST_ITEMS 8
+#endif
+#ifndef CG_HIST_MINB
+#define CG_HIST_MINB 4
+#endif
+constexpr int HIST_ITEMS = CG_HIST_ITEMS;    // items per thread per hist iteration (4-byte keys and weights)
+constexpr int HIST_MINB = CG_HIST_MINB;      // histogram CTAs per SM the register budget is sized for
 constexpr int CONV_TILE = 2 * BLOCK;          // points per k_convert tile
 constexpr int R_ITEMS = 8;                   // items per thread per reorder tile
 constexpr int R_TILE = BLOCK * R_ITEMS;      // 2048
@@ -188,6 +195,22 @@ __device__ __forceinline__ CtaRange cta_tiles(uint64_t ntiles, uint32_t b, uint3
 }
 
 __device__ __forceinline__ void atomic_max_ord(uint32_t *p, uint32_t v) { atomicMax(p, v); }
+
+// 64-bit add to shared memory from 32-bit atomics: sm_103 has no 64-bit
+// shared-memory add instruction (it becomes a compare-and-swap loop), while
+// 32-bit shared atomics are native.  The low word's old value tells whether
+// the add carried into the high word; once every add has landed the two words
+// hold the exact sum (mod 2^64).
+__device__ __forceinline__ void shared_add_u64(uint64_t *p, uint64_t v) {
+    uint32_t *w = (uint32_t *)p;
+    const uint32_t lo = (uint32_t)v;
+    uint32_t hi = (uint32_t)(v >> 32);
+    if (lo) {
+        const uint32_t old = atomicAdd(&w[0], lo);
+        hi += (uint32_t)(old + lo) < old ? 1u : 0u;
+    }
+    if (hi) atomicAdd(&w[1], hi);
+}
 __device__ __forceinline__ void atomic_max_ord(uint64_t *p, uint64_t v) {
     atomicMax((unsigned long long *)p, (unsigned long long)v);
 }
@@ -261,6 +284,12 @@ __device__ __forceinline__ uint64_t band_code(const BandSrc &bs, uint64_t orig, 
 // loops stay small (fewer branches and instruction-cache misses).
 static __device__ __noinline__ uint64_t band_code_cold(const BandSrc *bs, uint64_t orig, int coord) {
     return band_code(*bs, orig, coord);
+}
+// Inline for Rcb (a load), out of line for Rib's basis change (its nine
+// coefficients would otherwise hold registers across the caller's loop).
+__device__ __forceinline__ uint64_t band_code_lean(const BandSrc &bs, uint64_t orig, int coord) {
+    if (!bs.on) return KeyF64::from_f64(bs.pts[orig * (uint64_t)bs.D + coord]);
+    return band_code_cold(&bs, orig, coord);
 }
 
 // ---------------------------------------------------------------------------
@@ -741,6 +770,97 @@ __device__ __forceinline__ int bin_band_exact(int b, uint64_t c, const uint64_t 
     return b;
 }
 
+// ---------------------------------------------------------------------------
+// Bins without looking at the cuts.  With l, h the floats near the interval
+// ends and sc = nb / (h - l), a key k in [lo, hi] has the grid position
+// f = (approx(k) - l) * sc.  Every cut c_r lies within `dev` of the even grid
+// point l + (r+1)(h-l)/nb:
+//   KeyF32: each of the nbk f32 midpoints (a + b) / 2 of cuts within
+//           [lo, hi] adds at most half an ulp of M = max(|l|, |h|);
+//   KeyF64: f64 midpoints are exact to far below an f32 ulp, but l and h
+//           are truncated to f32 (one ulp of M) and so is approx(k);
+//   KeyBand: as KeyF64, plus one ulp for a cut's f32 band [RD32(c), RU32(c)].
+// f itself is (approx(k) - l) nb / (h - l) to 4 roundings of 2^-24, i.e. at
+// most (nb + 1) 2^-22 away for keys inside the interval (a subtraction with
+// a subnormal result is exact).  So when the fraction of f is more than
+// m = 2 (sc dev + (nb + 1) 2^-22) away from both bin edges (twice the bound),
+// floor(f) is the key's bin and, in the band form, the key is outside every
+// cut's band; the other keys take the exact search.  Intervals where m would
+// exceed 1/4 (narrow intervals far from zero, or ranges near the limits of
+// f32) use the exact search for every key (m = 2 never passes the test).
+// ---------------------------------------------------------------------------
+struct FastBin {
+    float l, sc, m, m1;  // m1 = 1 - m
+};
+template <class KT>
+__device__ __forceinline__ FastBin fast_bin(typename KT::C lo, typename KT::C hi, int nbk) {
+    FastBin r;
+    const float l = KT::approx_cut(lo), h = KT::approx_cut(hi);
+    const float nb = (float)(1 << nbk);
+    const float sc = nb / (h - l);
+    r.l = l;
+    r.sc = sc;
+    r.m = 2.0f;
+    r.m1 = -1.0f;
+    const float M = fmaxf(fabsf(l), fabsf(h));
+    if (!(h > l) || !isfinite(sc) || !(M > 1e-30f) || !(M < 1e37f)) return r;
+    // error of the cuts (and of approx(k)) in ulps of M
+    const float ulps = KT::BAND ? 4.0f : (sizeof(typename KT::T) == 8 ? 4.0f : (float)nbk);
+    const float u = M * 1.1920929e-7f + 1.4012985e-45f;  // >= ulp(M)
+    const float m = 2.0f * (sc * 1.01f * ulps * u + (nb + 1.0f) * 2.3841858e-7f);
+    if (m < 0.25f) {
+        r.m = m;
+        r.m1 = 1.0f - m;
+    }
+    return r;
+}
+
+// Keys that are certainly below every cut (bin 0) or at or above every cut
+// (the last bin): every cut lies in [lo, hi].  In the band form, by the f32
+// bounds of the f64 interval ends.
+template <class KT>
+struct EdgeTest {
+    typename KT::T lo, hi;
+    __device__ __forceinline__ bool below(typename KT::T k) const {
+        if constexpr (KT::BAND)
+            return k < lo;
+        else
+            return KT::lt(k, lo);
+    }
+    __device__ __forceinline__ bool above(typename KT::T k) const {
+        if constexpr (KT::BAND)
+            return k > hi;
+        else
+            return !KT::lt(k, hi);
+    }
+};
+template <class KT>
+__device__ __forceinline__ EdgeTest<KT> edge_test(typename KT::C lo, typename KT::C hi) {
+    EdgeTest<KT> e;
+    const typename KT::A M = fmax(fabs(KT::cval(lo)), fabs(KT::cval(hi)));
+    if (!isfinite(M + M)) {
+        // a midpoint may overflow to an infinite cut outside [lo, hi]: no
+        // shortcut (below: nothing is under -inf; above: only +inf, which
+        // is at or above every cut anyway; the band form: nothing above +inf)
+        if constexpr (KT::BAND) {
+            e.lo = -INFINITY;
+            e.hi = INFINITY;
+        } else {
+            e.lo = KT::cut_from_f64(-INFINITY);
+            e.hi = KT::cut_from_f64(INFINITY);
+        }
+        return e;
+    }
+    if constexpr (KT::BAND) {
+        e.lo = band_bounds(lo).lo;  // k < RD32(lo) proves x < lo
+        e.hi = band_bounds(hi).hi;  // k > RU32(hi) proves x > hi
+    } else {
+        e.lo = lo;
+        e.hi = hi;
+    }
+    return e;
+}
+
 // Global histogram slots: [segment][bin]; inv stores ~ord(key) so that an
 // all-zero slot means "no key" and atomicMax of ~ord is a min of keys.
 template <class KT, class WT>
@@ -770,7 +890,7 @@ __host__ __device__ constexpr int hist_max_nbk() {
 // shared-memory histogram flushed to the segment's global bins.
 // ---------------------------------------------------------------------------
 template <class KT, class WT>
-__global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
+__global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(const Seg<KT> *__restrict__ segs, const uint32_t *__restrict__ list,
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
@@ -784,16 +904,25 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
     constexpr int L = WT::LIMBS;
     constexpr int HNB = 1 << hist_max_nbk<WT>();
     constexpr int BNB = KT::BAND ? HNB : 1;
+    // items per thread per iteration: fewer with 8-byte keys or weights
+    // (registers)
+    constexpr int HI = (sizeof(K) == 4 && sizeof(typename WT::S) <= 4 && L == 1) ? HIST_ITEMS : HIST_ITEMS / 2;
+    // 16-bit weights: a bin is a 32-bit count and a 32-bit weight sum, each
+    // added by one native shared atomic, over windows of at most 2^15 items
+    // (sums below 2^31); other weights add 64-bit words from 32-bit atomics
+    constexpr bool C16 = sizeof(typename WT::S) == 2;
+    constexpr uint64_t WINDOW = C16 ? (1ull << 15) : PACK_WINDOW;
     __shared__ CK cuts[HNB];
     __shared__ float4 cbb[BNB];  // band form: f32 bounds of each bin (see build_sorted_cuts)
     __shared__ uint64_t sw[HNB * L];  // packed count|weight (L == 1 and !wide), else weight limbs
+    uint32_t *const sw32 = (uint32_t *)sw;  // 16-bit weights: 32-bit weight sums (counts in scnt)
     __shared__ uint32_t scnt[HNB];
     __shared__ O sinv[HNB];
-    // band form: each warp's queue of items whose f64 coordinate is needed
-    // (offsets in the piece), drained 32 at a time, one item per lane, so
-    // that their dependent loads overlap instead of stalling every iteration
-    constexpr int SLOWQ = KT::BAND ? 64 : 1;
-    __shared__ uint32_t s_q[KT::BAND ? NWARPS : 1][SLOWQ];
+    // each warp's queue of items that need the exact search over the cuts
+    // (band form: or their f64 coordinate), as offsets in the piece, drained
+    // 32 at a time, one item per lane, so that their dependent loads overlap
+    // instead of stalling every iteration
+    __shared__ uint32_t s_q[NWARPS][64];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int NB = 1 << nbk;
     int fs = L > 1 ? rs->fscale : 0;  // several sets: each set's own (set_fs)
@@ -883,13 +1012,16 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             } else {
                 bin = bin_sorted<KT>(kv, wc, NB, g);
             }
-            if (spk) {
-                atomicAdd((unsigned long long *)&wsw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
+            if (C16) {
+                atomicAdd(&wcnt[bin], 1u);
+                atomicAdd(&((uint32_t *)wsw)[bin], (uint32_t)q[0]);
+            } else if (spk) {
+                shared_add_u64(&wsw[bin], (1ull << PACK_SHIFT) | q[0]);
             } else {
                 atomicAdd(&wcnt[bin], 1u);
 #pragma unroll
                 for (int l = 0; l < L; ++l)
-                    if (q[l]) atomicAdd((unsigned long long *)&wsw[bin * L + l], (unsigned long long)q[l]);
+                    if (q[l]) shared_add_u64(&wsw[bin * L + l], q[l]);
             }
             const O v = (O)~KT::ord(kv);
             if (v > winv[bin]) atomic_max_ord(&winv[bin], v);
@@ -915,7 +1047,10 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         for (int i = lane; i < NB; i += 32) {
             uint32_t c;
             uint64_t wl[L];
-            if (spk) {
+            if (C16) {
+                c = wcnt[i];
+                wl[0] = ((uint32_t *)wsw)[i];
+            } else if (spk) {
                 c = (uint32_t)(wsw[i] >> PACK_SHIFT);
                 wl[0] = wsw[i] & PACK_WMASK;
 #pragma unroll
@@ -955,7 +1090,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             continue;
         }
         const uint32_t s = list[k];
-        const uint64_t pe = min(min(c1, P[k + 1]), pos + PACK_WINDOW);
+        const uint64_t pe = min(min(c1, P[k + 1]), pos + WINDOW);
         const Seg<KT> &sg = segs[s];
         if (L > 1 && set_fs) {
             fs = set_fs[sg.set];
@@ -1010,147 +1145,227 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         }
         __syncthreads();
         const BinGuess g = bin_guess<KT>(lo, hi, NB);
+        const FastBin fb = fast_bin<KT>(lo, hi, nbk);
+        const EdgeTest<KT> et = edge_test<KT>(lo, hi);
         bool xpend = false;  // band form: a decision waits for an exact minimum
         uint32_t xkey = 0;
         uint64_t xcut = 0;
         uint64_t xm = ~0ull;  // band form: this thread's part of that minimum
         uint32_t nband = 0;   // band form: f64 coordinates this thread read
-        uint32_t qn = 0;      // band form: entries in this warp's queue (same in every lane)
+        uint32_t qn = 0;      // entries in this warp's queue of exact-search items (same in every lane)
         if constexpr (KT::BAND) {
             xpend = sg.xstate == X_PENDING;
             xkey = sg.xkey;
             xcut = sg.xcut;
         }
-        // Keys below lo are all in bin 0 and keys >= hi all in bin NB-1 (every
-        // cut lies in [lo, hi]).  Once the interval has narrowed, most keys are
-        // there, so they are summed in registers instead of by atomics.
+        // The first and last bins take every key below the first cut and at
+        // or above the last one.  Once the interval has narrowed, most keys
+        // are there, so their sums stay in registers instead of atomics.
         uint32_t out_c[2] = {0, 0};
         uint64_t out_w[2][L];
         O out_inv[2] = {0, 0};
 #pragma unroll
         for (int l = 0; l < L; ++l) out_w[0][l] = out_w[1][l] = 0;
-        // band form: one queued item (its key, weight and f64 coordinate)
-        auto band_item = [&](uint64_t e) {
-            if constexpr (KT::BAND) {
-                const K kk = keys[e];
-                const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
-                ++nband;
-                if (xpend && KT::ord(kk) == xkey && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
-                uint64_t q[L];
-                item_q(wts[e], q);
-                const O v = (O)~KT::ord(kk);
-                const bool below = KeyF64::lt(c, lo), above = !below && !KeyF64::lt(c, hi);
-                if (below) {
+        // adds a key of bin `bin` (weight limbs q, inverted key v)
+        auto add_bin = [&](int bin, const uint64_t *q, O v) {
+            if (bin == 0 || bin == NB - 1) {
+                // constant indices only: keeps the sums in registers
+                if (bin == 0) {
                     out_c[0] += 1;
 #pragma unroll
                     for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
                     out_inv[0] = v > out_inv[0] ? v : out_inv[0];
-                    return;
-                }
-                if (above) {
+                } else {
                     out_c[1] += 1;
 #pragma unroll
                     for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
                     out_inv[1] = v > out_inv[1] ? v : out_inv[1];
-                    return;
                 }
-                bool unused;
-                const int bin = bin_band_exact(bin_band<KT>(kk, cuts, cbb, NB, g, unused), c, cuts, NB);
-                if (packed) {
-                    atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
-                } else {
-                    atomicAdd(&scnt[bin], 1u);
-#pragma unroll
-                    for (int l = 0; l < L; ++l)
-                        if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
-                }
-                if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+                return;
             }
+            if (C16) {
+                atomicAdd(&scnt[bin], 1u);
+                atomicAdd(&sw32[bin], (uint32_t)q[0]);
+            } else if (packed) {
+                shared_add_u64(&sw[bin], (1ull << PACK_SHIFT) | q[0]);
+            } else {
+                atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                for (int l = 0; l < L; ++l)
+                    if (q[l]) shared_add_u64(&sw[bin * L + l], q[l]);
+            }
+            if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
         };
-        for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HIST_ITEMS) {
-            // items of this iteration: 32-bit offsets from base below lim
-            const uint32_t lim = (uint32_t)min((uint64_t)BLOCK * HIST_ITEMS, b - base);
-            K kv[HIST_ITEMS];
-            typename WT::S wv[HIST_ITEMS];
-#pragma unroll
-            for (int i = 0; i < HIST_ITEMS; ++i) {
-                const uint32_t li = i * BLOCK + threadIdx.x;
-                if (li < lim) {
-                    kv[i] = keys[base + li];
-                    wv[i] = wts[base + li];
-                }
-            }
+        // one queued item: the exact search over the cuts (and in the band
+        // form, the f64 coordinate when the key is in a cut's band or is the
+        // key a decision waits for)
+        auto slow_item = [&](uint64_t e) {
+            const K kk = keys[e];
+            uint64_t q[L];
+            item_q(wts[e], q);
+            int bin;
             if constexpr (KT::BAND) {
-                // f32 keys against f64 cuts: the key decides, except in the
-                // band.  Items in a band (or the key a decision of this segment
-                // waits for) are only marked here, so that this unrolled loop
-                // stays small and keeps the keys in registers; the loop after
-                // it reads their f64 coordinate.
-                uint32_t slow = 0;
+                bool in_band;
+                bin = bin_band<KT>(kk, cuts, cbb, NB, g, in_band);
+                const bool pend = xpend && KT::ord(kk) == xkey;
+                if (in_band || pend) {
+                    const uint64_t c = band_code(bs, isrc ? isrc[e] : e, coord);
+                    ++nband;
+                    if (pend && !KeyF64::lt(c, xcut)) xm = c < xm ? c : xm;
+                    bin = bin_band_exact(bin, c, cuts, NB);
+                }
+            } else {
+                bin = bin_sorted<KT>(kk, cuts, NB, g);
+            }
+            add_bin(bin, q, (O)~KT::ord(kk));
+        };
+        // Passes after the first of a level search a narrowed interval: most
+        // keys then fall outside it, into the first and last bins, whose sums
+        // stay in registers (atomics on two words would serialise).  A
+        // level's first pass spans the whole interval and adds those two
+        // bins like any other.
+        const bool ER = sg.steps != 0;    // edge bins in registers (uniform)
+        const bool PD = KT::BAND && xpend;  // a decision waits for a key's exact minimum (uniform)
+        {
+            for (uint64_t base = a; base < b; base += (uint64_t)BLOCK * HI) {
+                // items of this iteration: 32-bit offsets from base below lim
+                const uint32_t lim = (uint32_t)min((uint64_t)BLOCK * HI, b - base);
+                const K *kb = keys + base;
+                const typename WT::S *wb = wts + base;
+                K kv[HI];
+                typename WT::S wv[HI];
 #pragma unroll
-                for (int i = 0; i < HIST_ITEMS; ++i) {
+                for (int i = 0; i < HI; ++i) {
                     const uint32_t li = i * BLOCK + threadIdx.x;
-                    if (L > 1 && accx && li < lim && KT::isnan(kv[i])) {
+                    if (li < lim) {
+                        kv[i] = kb[li];
+                        wv[i] = wb[li];
+                    }
+                }
+                // Bins from the grid position (fast_bin); the few items whose
+                // position is too close to a bin edge take the exact search in
+                // place.  Band-form items in a cut's band (and items whose key
+                // a decision waits for) are only marked here and resolved from
+                // the warp's queue, 32 at a time, so that their dependent f64
+                // loads overlap.
+                uint32_t slow = 0;
+                int bins[HI];     // bin of an item to add by atomics (-1: none)
+                uint32_t qlo[HI];  // f64 weights in packed bins: the truncated fixed-point weight
+#pragma unroll
+                for (int i = 0; i < HI; ++i) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    const bool valid = li < lim;
+                    const bool nan = KT::isnan(kv[i]);
+                    if (L > 1 && accx && valid && nan) {
                         uint64_t q[L];
                         item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
                     }
-                    if (li < lim && !KT::isnan(kv[i])) {
-                        if (xpend && KT::ord(kv[i]) == xkey) {
-                            slow |= 1u << i;
-                            continue;
+                    const bool binned = valid && !nan;
+                    const bool below = et.below(kv[i]), above = !below && et.above(kv[i]);
+                    const float f = (KT::approx(kv[i]) - fb.l) * fb.sc;
+                    const int bg = __float2int_rz(f);
+                    const float fr = f - (float)bg;
+                    const bool fast = (uint32_t)bg < (uint32_t)NB && fr > fb.m && fr < fb.m1;
+                    int bin = below ? 0 : (above ? NB - 1 : bg);
+                    bool sl = false;  // queued for its f64 coordinate (band form)
+                    if (binned && !below && !above && !fast) {
+                        // rare: the exact search over the cuts, in place
+                        if constexpr (KT::BAND) {
+                            bool in_band;
+                            bin = bin_band<KT>(kv[i], cuts, cbb, NB, g, in_band);
+                            sl = in_band;
+                        } else {
+                            bin = bin_sorted<KT>(kv[i], cuts, NB, g);
                         }
-                        // keys outside the interval land in the edge bins like
-                        // their neighbours inside it; edge-bin sums stay in
-                        // registers (most keys once the interval has narrowed)
-                        bool in_band;
-                        const int bin = bin_band<KT>(kv[i], cuts, cbb, NB, g, in_band);
-                        if (in_band) {
-                            slow |= 1u << i;
-                            continue;
+                    }
+                    if (PD) sl = sl || (binned && KT::ord(kv[i]) == xkey);
+                    slow |= (uint32_t)sl << i;
+                    const bool take = binned && !sl;
+                    const bool edge = ER && take && (bin == 0 || bin == NB - 1);
+                    bins[i] = take && !edge ? bin : -1;
+                    qlo[i] = 0;
+                    if constexpr (L == 1) {
+                        if (ER) {
+                            uint64_t q[1];
+                            WT::limbs(wv[i], fs, q);
+                            const O v = (O)~KT::ord(kv[i]);
+                            const bool e0 = edge && bin == 0, e1 = edge && bin != 0;
+                            out_c[0] += e0 ? 1u : 0u;
+                            out_w[0][0] += e0 ? q[0] : 0ull;
+                            out_inv[0] = e0 && v > out_inv[0] ? v : out_inv[0];
+                            out_c[1] += e1 ? 1u : 0u;
+                            out_w[1][0] += e1 ? q[0] : 0ull;
+                            out_inv[1] = e1 && v > out_inv[1] ? v : out_inv[1];
                         }
+                    } else if (take) {
                         uint64_t q[L];
                         item_q(wv[i], q);
-                        const O v = (O)~KT::ord(kv[i]);
-                        if (bin == 0 || bin == NB - 1) {
-                            // constant indices only: keeps the sums in registers
-                            if (bin == 0) {
-                                out_c[0] += 1;
-#pragma unroll
-                                for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
-                                out_inv[0] = v > out_inv[0] ? v : out_inv[0];
-                            } else {
-                                out_c[1] += 1;
-#pragma unroll
-                                for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
-                                out_inv[1] = v > out_inv[1] ? v : out_inv[1];
-                            }
-                            continue;
-                        }
-                        if (packed) {
-                            atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
-                        } else {
-                            atomicAdd(&scnt[bin], 1u);
-#pragma unroll
-                            for (int l = 0; l < L; ++l)
-                                if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
-                        }
-                        if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
+                        qlo[i] = (uint32_t)q[0];
+                        if (edge) add_bin(bin, q, (O)~KT::ord(kv[i]));
                     }
                 }
-                if (__any_sync(0xffffffffu, slow != 0)) {
+                // the bins' current minima first (independent loads in flight
+                // together), then the adds; a minimum read before another
+                // thread lowered it only costs an extra atomic
+                O old[HI];
+#pragma unroll
+                for (int i = 0; i < HI; ++i) old[i] = bins[i] >= 0 ? sinv[bins[i]] : (O)~(O)0;
+#pragma unroll
+                for (int i = 0; i < HI; ++i) {
+                    const int bin = bins[i];
+                    if (bin < 0) continue;
+                    if (C16) {
+                        atomicAdd(&scnt[bin], 1u);
+                        atomicAdd(&sw32[bin], (uint32_t)wv[i]);
+                    } else if (packed) {
+                        uint64_t w0;
+                        if constexpr (L == 1) {
+                            uint64_t q[1];
+                            WT::limbs(wv[i], fs, q);
+                            w0 = q[0];
+                        } else {
+                            w0 = qlo[i];
+                        }
+                        shared_add_u64(&sw[bin], (1ull << PACK_SHIFT) | w0);
+                    } else {
+                        uint64_t q[L];
+                        if constexpr (L == 1) {
+                            WT::limbs(wv[i], fs, q);
+                        } else {
+                            const unsigned __int128 qq = fixed_q_bits((double)wv[i], fs);
+                            q[0] = (uint32_t)qq;
+                            q[1] = (uint32_t)(qq >> 32);
+                            q[2] = (uint32_t)(qq >> 64);
+                            q[3] = (uint32_t)(qq >> 96);
+                        }
+                        atomicAdd(&scnt[bin], 1u);
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            if (q[l]) shared_add_u64(&sw[bin * L + l], q[l]);
+                    }
+                    const O v = (O)~KT::ord(kv[i]);
+                    if (v > old[i]) atomic_max_ord(&sinv[bin], v);
+                }
+                // queue the marked items; every 32 of them are searched, one
+                // per lane, and on the last iteration the queue's rest (a
+                // single call site keeps the search's registers out of the
+                // loop above)
+                const bool fin = base + (uint64_t)BLOCK * HI >= b;
+                if (__any_sync(0xffffffffu, slow != 0) || (fin && qn)) {
 #pragma unroll 1
-                    for (int i = 0; i < HIST_ITEMS; ++i) {
-                        const bool bit = (slow >> i) & 1u;
+                    for (int i = 0; i <= HI; ++i) {
+                        const bool bit = i < HI && ((slow >> i) & 1u);
                         const uint32_t m = __ballot_sync(0xffffffffu, bit);
                         if (bit)
                             s_q[warp][qn + __popc(m & ((1u << lane) - 1))] =
                                 (uint32_t)(base - a) + i * BLOCK + threadIdx.x;
                         qn += __popc(m);
-                        if (qn >= 32) {
+                        if (qn >= 32 || (i == HI && fin && qn)) {
+                            const uint32_t cnt = qn < 32 ? qn : 32u;
                             __syncwarp();
-                            band_item(a + s_q[warp][lane]);
+                            if (lane < cnt) slow_item(a + s_q[warp][lane]);
                             // keep the rest (fewer than 32) at the front
-                            qn -= 32;
+                            qn -= cnt;
                             const uint32_t v = lane < qn ? s_q[warp][32 + lane] : 0u;
                             __syncwarp();
                             if (lane < qn) s_q[warp][lane] = v;
@@ -1158,54 +1373,6 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
                         __syncwarp();
                     }
                 }
-                continue;
-            } else {
-#pragma unroll
-            for (int i = 0; i < HIST_ITEMS; ++i) {
-                const uint32_t li = i * BLOCK + threadIdx.x;
-                if (L > 1 && accx && li < lim && KT::isnan(kv[i])) {
-                    uint64_t q[L];
-                    item_q(wv[i], q);  // a NaN key is not binned; its weight is in the sum
-                }
-                if (li < lim && !KT::isnan(kv[i])) {
-                    uint64_t q[L];
-                    item_q(wv[i], q);
-                    const bool below = KT::lt(kv[i], lo), above = !below && !KT::lt(kv[i], hi);
-                    if (below || above) {
-                        // constant indices only: keeps the sums in registers
-                        const O v = (O)~KT::ord(kv[i]);
-                        if (below) {
-                            out_c[0] += 1;
-#pragma unroll
-                            for (int l = 0; l < L; ++l) out_w[0][l] += q[l];
-                            out_inv[0] = v > out_inv[0] ? v : out_inv[0];
-                        } else {
-                            out_c[1] += 1;
-#pragma unroll
-                            for (int l = 0; l < L; ++l) out_w[1][l] += q[l];
-                            out_inv[1] = v > out_inv[1] ? v : out_inv[1];
-                        }
-                        continue;
-                    }
-                    const int bin = bin_sorted<KT>(kv[i], cuts, NB, g);
-                    if (packed) {
-                        atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((1ull << PACK_SHIFT) | q[0]));
-                    } else {
-                        atomicAdd(&scnt[bin], 1u);
-#pragma unroll
-                        for (int l = 0; l < L; ++l)
-                            if (q[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)q[l]);
-                    }
-                    const O v = (O)~KT::ord(kv[i]);
-                    if (v > sinv[bin]) atomic_max_ord(&sinv[bin], v);
-                }
-            }
-            }
-        }
-        if constexpr (KT::BAND) {
-            if (qn) {
-                if (lane < qn) band_item(a + s_q[warp][lane]);  // the queue's rest
-                __syncwarp();
             }
         }
         if constexpr (L > 1) {
@@ -1237,13 +1404,16 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
             const O inv = (O)~warp_min_ord<O>((O)~out_inv[side]);
             if ((threadIdx.x & 31) == 0 && c) {
                 const int bin = side == 0 ? 0 : NB - 1;
-                if (packed) {
-                    atomicAdd((unsigned long long *)&sw[bin], (unsigned long long)((c << PACK_SHIFT) | wsum[0]));
+                if (C16) {
+                    atomicAdd(&scnt[bin], (uint32_t)c);
+                    atomicAdd(&sw32[bin], (uint32_t)wsum[0]);
+                } else if (packed) {
+                    shared_add_u64(&sw[bin], (c << PACK_SHIFT) | wsum[0]);
                 } else {
                     atomicAdd(&scnt[bin], (uint32_t)c);
 #pragma unroll
                     for (int l = 0; l < L; ++l)
-                        if (wsum[l]) atomicAdd((unsigned long long *)&sw[bin * L + l], (unsigned long long)wsum[l]);
+                        if (wsum[l]) shared_add_u64(&sw[bin * L + l], wsum[l]);
                 }
                 atomic_max_ord(&sinv[bin], inv);
             }
@@ -1252,7 +1422,10 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : 4) k_hist(const Seg
         for (int i = threadIdx.x; i < NB; i += BLOCK) {
             uint32_t c;
             uint64_t wl[L];
-            if (packed) {
+            if (C16) {
+                c = scnt[i];
+                wl[0] = sw32[i];
+            } else if (packed) {
                 c = (uint32_t)(sw[i] >> PACK_SHIFT);
                 wl[0] = sw[i] & PACK_WMASK;
 #pragma unroll
