@@ -1274,6 +1274,16 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                             bool in_band;
                             bin = bin_band<KT>(kv[i], cuts, cbb, NB, g, in_band);
                             sl = in_band;
+                        } else if (fb.m < 1.0f) {
+                            // the grid position is within m/2 of the key's
+                            // and every cut within m/2 of its grid point
+                            // (m < 1/4): the bin is bg - 1, bg or bg + 1
+                            const int b0 = min(max(bg, 0), NB - 1);
+                            bin = b0;
+                            if (b0 > 0 && KT::lt(kv[i], cuts[b0 - 1]))
+                                bin = b0 - 1;
+                            else if (b0 < NB - 1 && !KT::lt(kv[i], cuts[b0]))
+                                bin = b0 + 1;
                         } else {
                             bin = bin_sorted<KT>(kv[i], cuts, NB, g);
                         }
