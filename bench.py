@@ -468,8 +468,19 @@ def run_workload(args):
             return {3: out.cpu().numpy().view(np.uint64).copy()}
 
         def cpu_run():
-            return {3: (oracle.rib if rib else oracle.rcb)(pts_h, w_h, iters, tol, threads=0)[0]}
+            # the reference's arithmetic: f64 weights summed in f64, in
+            # chunks as rayon's fold and reduce do (threads=0: all cores);
+            # Rib given the GPU's basis change, so that the comparison of
+            # the ids isolates the weight sums
+            kw = dict(fsum=oracle.FSUM_SEQ, threads=0, splits=True)
+            if rib:
+                kw["matrix"] = coupe.rib_matrix_device(p_d)
+            r, st = (oracle.rib if rib else oracle.rcb)(pts_h, w_h, iters, tol, **kw)
+            cpu_stats.update(st)
+            cpu_stats["matrix"] = kw.get("matrix")
+            return {3: r}
     t_gen = time.perf_counter() - t_gen
+    cpu_stats = {}
     tuned = None
     if args.workload == "batched4096":
         # the schedule for this batch, picked by the library's autotuner
@@ -555,11 +566,37 @@ def run_workload(args):
         ref = cpu_run()
         t_cpu = time.perf_counter() - t0
         parity["ref32_vs_oracle_mismatches"] = int(sum((ref[d] != got["ref32"][d]).sum() for d in ref))
+        sample = "full workload, one run (%.2f s); OpenMP restatement of coupe %s" % (t_cpu, cfg.get("algorithm", "Rcb"))
+        if args.workload != "batched4096":
+            import float_parity
+            sample += ("; f64 weights summed in f64 in rayon-like chunks (the reference's arithmetic)"
+                       + ("; given the GPU's basis change" if args.workload == "hexrib134M" else ""))
+            # float-weight criteria of the GPU (REF32) against the reference's f64 sums
+            M = cpu_stats.get("matrix")
+            keys = (oracle.map_points(hosts[3][0], M) if M is not None else hosts[3][0]).astype(np.float32)
+            crit = float_parity.compare(got["ref32"][3], ref[3], keys, hosts[3][1], cfg["iter_count"], tol,
+                                        cpu_stats["split_pos"])
+            crit.pop("mismatch_nodes", None)
+            parity["vs_reference_f64_sums"] = crit
         cpu = {"value": round(n / t_cpu / 1e6, 2), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-               "sample": "full workload, one run (%.2f s); OpenMP restatement of coupe %s" %
-                         (t_cpu, cfg.get("algorithm", "Rcb"))}
+               "sample": sample}
     ms = results["f32key_f64band"]
     h2d = sum(p.nbytes + w.nbytes for p, w in hosts.values())
+    wsum = None
+    if args.workload != "batched4096":
+        # the run's total weight against an FP64 oracle: the exact sum (the
+        # oracle's 128-bit fixed point, rounded once) and the reference's
+        # chunked f64 sum
+        step("f32key_f64band")
+        torch.cuda.synchronize()
+        st = coupe.last_stats()
+        w_h = hosts[3][1]
+        exact = oracle.fixed_sum(w_h, oracle.fixed_scale(w_h))
+        wsum = {"gpu": st["root_weight_sum"], "exact": exact, "gpu_error": st["root_weight_sum"] - exact,
+                "gpu_error_bound": st["weight_sum_error_bound"]}
+        if "root_sum" in cpu_stats:
+            wsum["reference_f64"] = cpu_stats["root_sum"]
+            wsum["reference_f64_error"] = cpu_stats["root_sum"] - exact
     line = {
         "metric": "%s Mpoints/s, %s: FP32-key+FP64-band vs plain FP64 on GB300" % (
             cfg.get("algorithm", "RCB").upper(), cfg["workload"]),
@@ -577,6 +614,8 @@ def run_workload(args):
                                        for m, pr in by_mode.items()}},
         "clocks": clocks.summary() if clocks else None, "generation_s": round(t_gen, 1), "autotune": tuned,
     }
+    if wsum:
+        line["weight_sum"] = wsum
     if cpu:
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)

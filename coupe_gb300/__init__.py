@@ -59,7 +59,8 @@ class Stats(ctypes.Structure):
         "points", "levels", "splits", "split_steps", "max_split_steps", "hist_passes",
         "hist_points", "band_points", "kernel_launches", "algo_bytes")] + [
         ("root_weight_sum", ctypes.c_double), ("device_ms", ctypes.c_double),
-        ("fixed_scale", ctypes.c_int), ("mode", ctypes.c_int), ("weight_rechecks", ctypes.c_uint64)]
+        ("fixed_scale", ctypes.c_int), ("mode", ctypes.c_int), ("weight_rechecks", ctypes.c_uint64),
+        ("weight_sum_error_bound", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

@@ -116,6 +116,12 @@ DevCtx *device_ctx(std::string *err) {
 }
 
 int ensure_workspace(DevCtx &C, size_t bytes, std::string *err) {
+    const int lim = tuning().workspace_limit_mb;
+    if (lim > 0 && bytes > ((size_t)lim << 20)) {
+        *err = "workspace of " + std::to_string(bytes) + " bytes exceeds the limit of " + std::to_string(lim) +
+               " MiB (option workspace_limit_mb)";
+        return COUPE_ERR_ALLOC;
+    }
     if (bytes <= C.ws_cap) return COUPE_ERR_OK;
     if (C.ws) {
         cudaStreamSynchronize(C.stream);

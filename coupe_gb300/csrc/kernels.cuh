@@ -39,7 +39,6 @@ constexpr int R_TILE = BLOCK * R_ITEMS;      // 2048
 constexpr uint64_t LB_AGG = 1ull << 62;      // look-back: aggregate published
 constexpr uint64_t LB_INCL = 2ull << 62;     // look-back: inclusive prefix published
 constexpr uint64_t LB_VALUE = (1ull << 62) - 1;
-constexpr uint32_t LB_SPIN_LIMIT = 1u << 22;
 constexpr int PACK_WBITS_IN = 20;            // packed histograms take weights below 2^20
 
 // ---------------------------------------------------------------------------
@@ -720,10 +719,10 @@ __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT:
     if (g.fast) {
         float f = (KT::approx(key) - g.lo) * g.scale;
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
-        int b = __float2int_rz(f);
-        while (b > 0 && KT::lt(key, cuts[b - 1])) --b;
-        while (b < nb - 1 && !KT::lt(key, cuts[b])) ++b;
-        return b;
+        const int b = __float2int_rz(f);
+        // the guess, if its two cuts confirm it; else the binary search
+        // (cuts crowded at the precision of the keys make the guess far off)
+        if ((b == 0 || !KT::lt(key, cuts[b - 1])) && (b == nb - 1 || KT::lt(key, cuts[b]))) return b;
     }
     int l = 0, r = nb - 1;
     while (l < r) {
@@ -742,12 +741,19 @@ __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT:
 template <class KT>
 __device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const float4 *cbb, int nb,
                                         const BinGuess &g, bool &in_band) {
-    int b;
+    int b = -1;
+    float4 q;
     if (g.fast) {
         float f = (k - g.lo) * g.scale;
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
         b = __float2int_rz(f);
-    } else {
+        q = cbb[b];
+        // the guess stands if the bounds of its two cuts confirm it
+        if (!((b == 0 || k > q.x) && (b == nb - 1 || !(k > q.y)))) b = -1;
+    }
+    if (b < 0) {
+        // binary search: the first bin whose upper cut bound is >= k (a
+        // narrow interval crowds many cuts into one f32 value)
         int l = 0, r = nb - 1;
         while (l < r) {
             const int m = (l + r) >> 1;
@@ -757,16 +763,22 @@ __device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const flo
                 r = m;
         }
         b = l;
+        q = cbb[b];
     }
-    float4 q = cbb[b];
-    while (b > 0 && !(k > q.x)) q = cbb[--b];
-    while (b < nb - 1 && k > q.y) q = cbb[++b];
     in_band = q.w != 0.f && !(k < q.z);  // cut b's band: finish with bin_band_exact
     return b;
 }
-// The bin from cut b on, from the f64 code.
+// The bin from cut b on, from the f64 code: the first cut above c, by binary
+// search (a narrow interval can hold hundreds of cuts within one f32 band).
 __device__ __forceinline__ int bin_band_exact(int b, uint64_t c, const uint64_t *cuts, int nb) {
-    while (b < nb - 1 && !KeyF64::lt(c, cuts[b])) ++b;
+    int r = nb - 1;  // answer in [b, r]
+    while (b < r) {
+        const int m = (b + r) >> 1;
+        if (KeyF64::lt(c, cuts[m]))
+            r = m;
+        else
+            b = m + 1;
+    }
     return b;
 }
 
@@ -1269,7 +1281,8 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                     int bin = below ? 0 : (above ? NB - 1 : bg);
                     bool sl = false;  // queued for its f64 coordinate (band form)
                     if (binned && !below && !above && !fast) {
-                        // rare: the exact search over the cuts, in place
+                        // rare: the exact search over the cuts, in place (the
+                        // neighbouring cuts, else a binary search)
                         if constexpr (KT::BAND) {
                             bool in_band;
                             bin = bin_band<KT>(kv[i], cuts, cbb, NB, g, in_band);
@@ -1285,7 +1298,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                             else if (b0 < NB - 1 && !KT::lt(kv[i], cuts[b0]))
                                 bin = b0 + 1;
                         } else {
-                            bin = bin_sorted<KT>(kv[i], cuts, NB, g);
+                            bin = bin_sorted<KT>(kv[i], cuts, NB, BinGuess{0.f, 0.f, 0});
                         }
                     }
                     if (PD) sl = sl || (binned && KT::ord(kv[i]) == xkey);
@@ -2098,6 +2111,7 @@ struct ReorderArgs {
     uint64_t *lb;  // look-back words, one per chunk, zeroed
     RunScalars *rs;
     BandSrc bs;    // band form: the f64 coordinates (through isrc)
+    uint32_t spin_limit;  // polls of a look-back wait before it fails (ERR_LOOKBACK_TIMEOUT)
 };
 
 // One tile in shared memory: D key arrays and a weight array, each with 16
@@ -2284,7 +2298,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
                     uint64_t v;
                     uint32_t spins = 0;
                     while ((v = *((volatile uint64_t *)&A.lb[j])) == 0) {
-                        if (++spins > LB_SPIN_LIMIT) break;
+                        if (++spins > A.spin_limit) break;
                         __nanosleep(64);
                     }
                     if (v == 0) {

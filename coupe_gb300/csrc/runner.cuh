@@ -416,6 +416,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         R.bs = bs;
         R.lb = B.lb;
         R.rs = B.rs;
+        R.spin_limit = (uint32_t)std::max(0, tu.lookback_spin_limit);
         const uint64_t rbytes = 2 * V * (D * sk + sw + si) - (ic ? 0 : V * si);
         const unsigned r_grid = (unsigned)std::min<uint64_t>(g_reorder, nchunks);
         if (carry) {
@@ -446,6 +447,13 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     {
         uint64_t lim[4] = {h_rs->wsum_limbs[0], h_rs->wsum_limbs[1], h_rs->wsum_limbs[2], h_rs->wsum_limbs[3]};
         st->root_weight_sum = WL::f64(WL::value(lim, h_rs->fscale));
+        st->weight_sum_error_bound = 0.0;
+        if (WL::LIMBS > 1) {
+            // n quantisation errors of at most 2^(-s-1), then one rounding
+            const double a = std::fabs(st->root_weight_sum);
+            st->weight_sum_error_bound =
+                (double)n * std::ldexp(1.0, -h_rs->fscale - 1) + 0.5 * (std::nextafter(a, INFINITY) - a);
+        }
     }
     // refinement passes: the points each scan left for the pass after it
     st->hist_points += h_rs->pass_points;

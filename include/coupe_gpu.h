@@ -47,6 +47,11 @@ struct coupe_gpu_stats {
 	int fixed_scale;          /* s of the 128-bit fixed-point weight sums */
 	int mode;                 /* enum coupe_gpu_mode used */
 	uint64_t weight_rechecks; /* f64 weights: decisions replayed with exact bins */
+	/* Bound on |root_weight_sum - the exact sum of the weights|: f64
+	 * weights are quantised to multiples of 2^-fixed_scale (at most half a
+	 * quantum each) and the exact fixed-point total is rounded once to f64;
+	 * 0 for integer weights (exact, wrapping sums). */
+	double weight_sum_error_bound;
 };
 
 /* coupe_rcb with an explicit precision mode. */

@@ -50,6 +50,8 @@ def lib():
         L.oracle_rcb.restype = i32
         L.oracle_rib.argtypes = [vp, u64, i32, vp, i32, vp, u64, dbl, i32, i32, i32, vp, ctypes.POINTER(Stats)]
         L.oracle_rib.restype = i32
+        L.oracle_record_splits.argtypes = [vp, u64]
+        L.oracle_record_splits.restype = None
         L.oracle_rib_matrix.argtypes = [u64, i32, vp, vp]
         L.oracle_rib_matrix.restype = i32
         L.oracle_map_points.argtypes = [vp, u64, i32, vp, vp]
@@ -79,17 +81,43 @@ def _prep(points, weights):
     return p, np.ascontiguousarray(w)
 
 
-def rcb(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1):
-    """Part ids (uint64) of coupe's Rcb, and run statistics."""
+class _SplitRecorder:
+    """Records the split position of every tree node (heap id) of one call."""
+
+    def __init__(self, iter_count):
+        self.buf = np.full((1 << (iter_count + 1)) - 1 if iter_count < 30 else 1, np.nan)
+
+    def __enter__(self):
+        lib().oracle_record_splits(self.buf.ctypes.data, len(self.buf))
+        return self.buf
+
+    def __exit__(self, *a):
+        lib().oracle_record_splits(None, 0)
+
+
+def rcb(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1, splits=False):
+    """Part ids (uint64) of coupe's Rcb, and run statistics; with splits=True
+    the statistics also hold "split_pos": the position of each node's split
+    by heap id (NaN where no split was made)."""
     p, w = _prep(points, weights)
     n, dim = p.shape
     out = np.zeros(n, dtype=np.uint64)
     st = Stats()
-    rc = lib().oracle_rcb(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
-                          iter_count, tolerance, mode, fsum, threads, ctypes.byref(st))
+    rec = _SplitRecorder(iter_count) if splits else None
+    if rec:
+        rec.__enter__()
+    try:
+        rc = lib().oracle_rcb(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
+                              iter_count, tolerance, mode, fsum, threads, ctypes.byref(st))
+    finally:
+        if rec:
+            rec.__exit__()
     if rc != 0:
         raise ValueError("oracle_rcb failed (%d)" % rc)
-    return out, st.as_dict()
+    d = st.as_dict()
+    if rec:
+        d["split_pos"] = rec.buf
+    return out, d
 
 
 def rcb_sets(points, weights, set_offsets, iter_counts, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1):
@@ -104,18 +132,29 @@ def rcb_sets(points, weights, set_offsets, iter_counts, tolerance, mode=REF32, f
     return out
 
 
-def rib(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1, matrix=None):
+def rib(points, weights, iter_count, tolerance, mode=REF32, fsum=FSUM_FIXED, threads=1, matrix=None,
+        splits=False):
     p, w = _prep(points, weights)
     n, dim = p.shape
     out = np.zeros(n, dtype=np.uint64)
     st = Stats()
     m = None if matrix is None else np.ascontiguousarray(np.asarray(matrix, dtype=np.float64))
-    rc = lib().oracle_rib(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
-                          iter_count, tolerance, mode, fsum, threads,
-                          m.ctypes.data if m is not None else None, ctypes.byref(st))
+    rec = _SplitRecorder(iter_count) if splits else None
+    if rec:
+        rec.__enter__()
+    try:
+        rc = lib().oracle_rib(out.ctypes.data, n, dim, p.ctypes.data, _WT[w.dtype], w.ctypes.data,
+                              iter_count, tolerance, mode, fsum, threads,
+                              m.ctypes.data if m is not None else None, ctypes.byref(st))
+    finally:
+        if rec:
+            rec.__exit__()
     if rc != 0:
         raise ValueError("oracle_rib failed (%d)" % rc)
-    return out, st.as_dict()
+    d = st.as_dict()
+    if rec:
+        d["split_pos"] = rec.buf
+    return out, d
 
 
 def rib_matrix(points):

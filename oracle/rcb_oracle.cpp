@@ -220,6 +220,11 @@ struct Items {
     }
 };
 
+// Where recurse records each split's position by heap id (oracle_record_splits;
+// the test of float-weight parity traces mismatching ids to these).
+static double *g_split_buf = nullptr;
+static uint64_t g_split_cap = 0;
+
 struct Ctx {
     int dim;
     double tol;
@@ -445,6 +450,7 @@ static void recurse(Ctx &cx, Items<K, WT> it, size_t iter_count, uint64_t iter_i
     const K mn = (K)bmin[coord];
     const K mx = (K)bmax[coord];
     SplitOut<K, WT> s = split<K, WT>(cx, it, coord, mn, mx, sum);
+    if (g_split_buf && iter_id < g_split_cap) g_split_buf[iter_id] = (double)s.split_pos;
     double lmin[3], lmax[3], rmin[3], rmax[3];
     for (int d = 0; d < 3; ++d) {
         lmin[d] = rmin[d] = bmin[d];
@@ -751,6 +757,14 @@ extern "C" {
 int oracle_rcb(uint64_t *part, uint64_t n, int dim, const double *pts, int wtype, const void *w,
                uint64_t iter_count, double tol, int mode, int fsum, int threads, oracle_stats *st) {
     return rcb_entry(part, n, dim, pts, wtype, w, iter_count, tol, mode, fsum, threads, st);
+}
+
+// The next oracle_rcb / oracle_rib call writes the position of the split of
+// tree node h (heap numbering, root 0) to buf[h] for h < cap (nodes it does
+// not split keep their value); buf == NULL stops recording.
+void oracle_record_splits(double *buf, uint64_t cap) {
+    g_split_buf = buf;
+    g_split_cap = buf ? cap : 0;
 }
 
 // The Rib basis change (OrientedBoundingBox::from_points, geometry.rs:210-228):
