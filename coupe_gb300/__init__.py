@@ -30,13 +30,14 @@ ERR_OK, ERR_ALLOC, ERR_CRASH, ERR_BAD_DIMENSION, ERR_BAD_TYPE, ERR_BIPART_ONLY, 
     ERR_LEN_MISMATCH, ERR_NOT_FOUND, ERR_NEG_VALUES = range(9)
 COUPE_INT, COUPE_INT64, COUPE_DOUBLE = 0, 1, 2
 MODES = {"ref32": 0, "f64": 1, "f32key_f64band": 2}
+WEIGHTED_INERTIA = 0x100  # COUPE_GPU_WEIGHTED_INERTIA (include/coupe_gpu.h): opt-in, Rib only
 
 # Symbols the library exports (checked by the CPU test-suite).
 EXPORTED = [
     "coupe_strerror", "coupe_data_free", "coupe_data_array", "coupe_data_constant",
     "coupe_data_fn", "coupe_rcb", "coupe_rib",
     "coupe_gpu_rcb", "coupe_gpu_rib", "coupe_gpu_rcb_device", "coupe_gpu_rib_device",
-    "coupe_gpu_rib_matrix", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
+    "coupe_gpu_rib_matrix", "coupe_gpu_rib_matrix_weighted", "coupe_gpu_last_stats", "coupe_gpu_last_error", "coupe_gpu_version",
     "coupe_gpu_profile", "coupe_gpu_profile_read", "coupe_gpu_kernel_name",
     "coupe_gpu_set_option", "coupe_gpu_get_option", "coupe_gpu_f64_to_f32",
     "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
@@ -114,6 +115,8 @@ def lib():
     L.coupe_gpu_autotune.restype = i32
     L.coupe_gpu_rib_matrix.argtypes = [u64, u64, vp, vp, vp]
     L.coupe_gpu_rib_matrix.restype = i32
+    L.coupe_gpu_rib_matrix_weighted.argtypes = [u64, u64, vp, i32, vp, vp, vp]
+    L.coupe_gpu_rib_matrix_weighted.restype = i32
     L.coupe_gpu_last_stats.argtypes = [ctypes.POINTER(Stats)]
     L.coupe_gpu_last_stats.restype = None
     L.coupe_gpu_last_error.argtypes = []
@@ -218,6 +221,7 @@ class _Bisection:
     iter_count: int = 0
     tolerance: float = 0.0
     mode: str = "ref32"
+    weighted_inertia: bool = False  # Rib only: weigh the inertia matrix by the weights (not coupe's default)
     _rib = False
 
     def partition(self, part_ids, data):
@@ -242,7 +246,8 @@ class _Bisection:
         dw = L.coupe_data_array(len(w), _weight_type(w), w.ctypes.data)
         try:
             fn = L.coupe_gpu_rib if self._rib else L.coupe_gpu_rcb
-            rc = fn(part_ids.ctypes.data, dim, dp, dw, self.iter_count, self.tolerance, MODES[self.mode])
+            mode = MODES[self.mode] | (WEIGHTED_INERTIA if self._rib and self.weighted_inertia else 0)
+            rc = fn(part_ids.ctypes.data, dim, dp, dw, self.iter_count, self.tolerance, mode)
         finally:
             L.coupe_data_free(dp)
             L.coupe_data_free(dw)
@@ -509,22 +514,31 @@ def barycentres_host(coords, nodes):
     return barycentres_device(c, v).cpu().numpy()
 
 
-def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None):
-    """Rib on CUDA tensors (see rcb_device)."""
+def rib_device(part_ids, points, weights, iter_count, tolerance, mode="ref32", stream=None,
+               weighted_inertia=False):
+    """Rib on CUDA tensors (see rcb_device).  weighted_inertia=True weighs
+    the inertia matrix by the weights (an opt-in; coupe's is unweighted)."""
     import torch
     n, dim = points.shape
     wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
     s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    m = MODES[mode] | (WEIGHTED_INERTIA if weighted_inertia else 0)
     rc = lib().coupe_gpu_rib_device(_ptr(part_ids), n, dim, _ptr(points), wt, _ptr(weights), iter_count,
-                                    tolerance, MODES[mode], ctypes.c_void_p(s))
+                                    tolerance, m, ctypes.c_void_p(s))
     _check(rc)
 
 
-def rib_matrix_device(points, stream=None):
-    """The Rib basis change (obb_to_aabb) of CUDA float64 points (N, D)."""
+def rib_matrix_device(points, stream=None, weights=None):
+    """The Rib basis change (obb_to_aabb) of CUDA float64 points (N, D); with
+    `weights` (a CUDA tensor) the weighted inertia's (an opt-in)."""
     import torch
     n, dim = points.shape
     out = np.zeros((dim, dim), dtype=np.float64)
     s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
-    _check(lib().coupe_gpu_rib_matrix(n, dim, _ptr(points), out.ctypes.data, ctypes.c_void_p(s)))
+    if weights is None:
+        _check(lib().coupe_gpu_rib_matrix(n, dim, _ptr(points), out.ctypes.data, ctypes.c_void_p(s)))
+    else:
+        wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
+        _check(lib().coupe_gpu_rib_matrix_weighted(n, dim, _ptr(points), wt, _ptr(weights), out.ctypes.data,
+                                                   ctypes.c_void_p(s)))
     return out

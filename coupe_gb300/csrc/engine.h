@@ -118,7 +118,7 @@ int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);
 
 // The Rib basis change (obb_to_aabb) of n device-resident points.
 int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
-               std::string *err);
+               std::string *err, int wtype = -1, const void *d_weights = nullptr);
 
 // Loads of parts 0..P-1 of a device-resident partition (coupe's
 // compute_parts_load), written to the host array `loads` (P elements of the

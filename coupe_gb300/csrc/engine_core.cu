@@ -168,48 +168,68 @@ int run_rcb(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) 
 
 // ---------------------------------------------------------------------------
 // Rib basis change.  inertia_matrix (geometry.rs:273-284) is unweighted: the
-// centroid sum(p)/n, then sum((p-c)(p-c)^T).  Both sums are reduced in a fixed
-// order (fixed grid, fixed tree inside each block, blocks summed in index
-// order on the host), so the result does not change from run to run.
+// centroid c = sum(p)/n, then M = sum((p-c)(p-c)^T).  One pass computes it:
+// with s = the first point, W = sum(w), S1 = sum(w (p - s)) and the upper
+// triangle of S2 = sum(w (p - s)(p - s)^T); then c = s + S1 / W and
+// M = S2 - S1 S1^T / W (w = 1 for coupe's matrix; the point weights for the
+// opt-in weighted inertia).  The shift keeps the subtraction well
+// conditioned.  Sums are reduced in a fixed order (fixed grid, fixed tree in
+// each block, blocks summed in index order on the host), so the result does
+// not change from run to run.  GB300 runs f64 arithmetic at a small fraction
+// of its integer rate and this pass is bound by it: the upper triangle halves
+// the products, and the one pass reads the points once.
 // ---------------------------------------------------------------------------
 constexpr int RIB_GRID = 1024;
 
 template <int D>
-__global__ void __launch_bounds__(BLOCK) k_moments(const double *__restrict__ pts, uint64_t n, const double *center,
-                                                   double *partial) {
-    __shared__ double sh[D * D][NWARPS];
-    double acc[D * D];
+__host__ __device__ constexpr int moment_terms() {
+    return 1 + D + D * (D + 1) / 2;  // W, S1, upper triangle of S2
+}
+
+template <int D, class WS>
+__global__ void __launch_bounds__(BLOCK) k_moments(const double *__restrict__ pts, uint64_t n,
+                                                   const WS *__restrict__ w, double *partial) {
+    constexpr int K = moment_terms<D>();
+    __shared__ double sh[K][NWARPS];
+    double acc[K];
 #pragma unroll
-    for (int k = 0; k < D * D; ++k) acc[k] = 0.0;
-    double c[D];
+    for (int k = 0; k < K; ++k) acc[k] = 0.0;
+    double sft[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) c[d] = center ? center[d] : 0.0;
+    for (int d = 0; d < D; ++d) sft[d] = pts[d];
     for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
-        double o[D];
+        double o[D], wo[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) o[d] = __dsub_rn(pts[i * D + d], c[d]);
-        if (!center) {
+        for (int d = 0; d < D; ++d) o[d] = __dsub_rn(pts[i * D + d], sft[d]);
+        if (w) {
+            const double wi = (double)w[i];
+            acc[0] = __dadd_rn(acc[0], wi);
 #pragma unroll
-            for (int d = 0; d < D; ++d) acc[d] = __dadd_rn(acc[d], o[d]);
+            for (int d = 0; d < D; ++d) wo[d] = __dmul_rn(wi, o[d]);
         } else {
 #pragma unroll
-            for (int a = 0; a < D; ++a)
-#pragma unroll
-                for (int b = 0; b < D; ++b) acc[a * D + b] = __dadd_rn(acc[a * D + b], __dmul_rn(o[a], o[b]));
+            for (int d = 0; d < D; ++d) wo[d] = o[d];
         }
+#pragma unroll
+        for (int d = 0; d < D; ++d) acc[1 + d] = __dadd_rn(acc[1 + d], wo[d]);
+        int k = 1 + D;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int b2 = a; b2 < D; ++b2, ++k) acc[k] = __dadd_rn(acc[k], __dmul_rn(wo[a], o[b2]));
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int K = center ? D * D : D;
+#pragma unroll
     for (int k = 0; k < K; ++k) {
         double v = acc[k];
-        for (int o = 16; o > 0; o >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+        for (int off = 16; off > 0; off >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
         if (lane == 0) sh[k][warp] = v;
     }
     __syncthreads();
     if (threadIdx.x < K) {
         double v = 0.0;
-        for (int w = 0; w < NWARPS; ++w) v = __dadd_rn(v, sh[threadIdx.x][w]);
-        partial[blockIdx.x * D * D + threadIdx.x] = v;
+        for (int w2 = 0; w2 < NWARPS; ++w2) v = __dadd_rn(v, sh[threadIdx.x][w2]);
+        partial[blockIdx.x * K + threadIdx.x] = v;
     }
 }
 
@@ -313,43 +333,57 @@ static bool obb_matrix(const double *inertia, int D, double *out) {
     return true;
 }
 
+template <int D, class WS>
+static int launch_moments(const double *d_points, uint64_t n, const WS *d_w, double *d_part, cudaStream_t s,
+                          std::string *err) {
+    k_moments<D, WS><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_w, d_part);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? (int)COUPE_ERR_OK : cuda_fail(e, "k_moments", err);
+}
+
 int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStream_t stream, double *out,
-               std::string *err) {
+               std::string *err, int wtype, const void *d_weights) {
     cudaStream_t s = stream ? stream : C.stream;
-    const size_t part_bytes = (size_t)RIB_GRID * 9 * sizeof(double);
-    int rc = ensure_workspace(C, part_bytes + 4 * sizeof(double), err);
+    const int K = dim == 2 ? moment_terms<2>() : moment_terms<3>();
+    const size_t part_bytes = (size_t)RIB_GRID * K * sizeof(double);
+    int rc = ensure_workspace(C, part_bytes, err);
     if (rc != COUPE_ERR_OK) return rc;
     double *d_part = (double *)C.ws;
-    double *d_c = d_part + RIB_GRID * 9;  // the centroid, after the partials
-    std::unique_ptr<double[]> h(new double[RIB_GRID * 9]);
-    double center[3] = {0, 0, 0};
-    // pass 1: centroid
+    std::unique_ptr<double[]> h(new double[RIB_GRID * K]);
+    const bool weighted = d_weights != nullptr;
+    if (!weighted) {
+        rc = dim == 2 ? launch_moments<2, double>(d_points, n, nullptr, d_part, s, err)
+                      : launch_moments<3, double>(d_points, n, nullptr, d_part, s, err);
+    } else if (wtype == COUPE_INT) {
+        rc = dim == 2 ? launch_moments<2>(d_points, n, (const int32_t *)d_weights, d_part, s, err)
+                      : launch_moments<3>(d_points, n, (const int32_t *)d_weights, d_part, s, err);
+    } else if (wtype == COUPE_INT64) {
+        rc = dim == 2 ? launch_moments<2>(d_points, n, (const int64_t *)d_weights, d_part, s, err)
+                      : launch_moments<3>(d_points, n, (const int64_t *)d_weights, d_part, s, err);
+    } else {
+        rc = dim == 2 ? launch_moments<2>(d_points, n, (const double *)d_weights, d_part, s, err)
+                      : launch_moments<3>(d_points, n, (const double *)d_weights, d_part, s, err);
+    }
+    if (rc != COUPE_ERR_OK) return rc;
     cudaError_t e;
-    if (dim == 2)
-        k_moments<2><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, nullptr, d_part);
-    else
-        k_moments<3><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, nullptr, d_part);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_moments", err);
-    if ((e = cudaMemcpyAsync(h.get(), d_part, part_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(s)) != cudaSuccess)
-        return cuda_fail(e, "centroid", err);
-    for (int b = 0; b < RIB_GRID; ++b)
-        for (int d = 0; d < dim; ++d) center[d] += h[b * dim * dim + d];
-    for (int d = 0; d < dim; ++d) center[d] = center[d] / (double)n;
-    // pass 2: second moments about the centroid
-    if ((e = cudaMemcpyAsync(d_c, center, 3 * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_fail(e, "centroid upload", err);
-    if (dim == 2)
-        k_moments<2><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_c, d_part);
-    else
-        k_moments<3><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_c, d_part);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_moments", err);
     if ((e = cudaMemcpyAsync(h.get(), d_part, part_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
         (e = cudaStreamSynchronize(s)) != cudaSuccess)
         return cuda_fail(e, "inertia", err);
-    double m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double t[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int b = 0; b < RIB_GRID; ++b)
-        for (int k = 0; k < dim * dim; ++k) m[k] += h[b * dim * dim + k];
+        for (int k = 0; k < K; ++k) t[k] += h[b * K + k];
+    const double W = weighted ? t[0] : (double)n;
+    if (!(W > 0.0) || !std::isfinite(W)) {
+        if (err) *err = "weighted inertia needs a positive finite weight sum";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    double m[9];
+    int k = 1 + dim;
+    for (int a = 0; a < dim; ++a)
+        for (int b = a; b < dim; ++b, ++k) {
+            const double v = t[k] - t[1 + a] * t[1 + b] / W;
+            m[a * dim + b] = m[b * dim + a] = v;
+        }
     if (!obb_matrix(m, dim, out)) {
         if (err) *err = "singular basis change";
         return COUPE_ERR_CRASH;

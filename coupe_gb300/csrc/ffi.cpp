@@ -122,6 +122,8 @@ coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const c
                     const coupe_data *weights, uintptr_t iter_count, double tolerance, int mode) {
     t_err.clear();
     std::memset(&t_stats, 0, sizeof(t_stats));
+    const bool winert = rib && (mode & COUPE_GPU_WEIGHTED_INERTIA) != 0;
+    mode &= ~COUPE_GPU_WEIGHTED_INERTIA;
     t_stats.mode = mode;
     if (!points || !weights) {
         t_err = "NULL data set";
@@ -214,7 +216,9 @@ coupe_err host_call(bool rib, uintptr_t *partition, uintptr_t dimension, const c
     int rc = COUPE_ERR_OK;
     if (rib) {
         double M[9];
-        rc = cg::rib_matrix(*C, n, (int)dimension, d_pts, s, M, &err);
+        if (winert) cudaStreamWaitEvent(s, C->ev_w, 0);  // the weights' upload
+        rc = winert ? cg::rib_matrix(*C, n, (int)dimension, d_pts, s, M, &err, weights->type, d_w)
+                    : cg::rib_matrix(*C, n, (int)dimension, d_pts, s, M, &err);
         if (rc == COUPE_ERR_OK) {
             a.has_matrix = true;
             std::memcpy(a.matrix, M, sizeof(M));
@@ -238,6 +242,8 @@ coupe_err device_call(bool rib, uint64_t *d_partition, uint64_t n, uint64_t dime
                       const double *matrix, void *stream) {
     t_err.clear();
     std::memset(&t_stats, 0, sizeof(t_stats));
+    const bool winert = rib && (mode & COUPE_GPU_WEIGHTED_INERTIA) != 0;
+    mode &= ~COUPE_GPU_WEIGHTED_INERTIA;
     t_stats.mode = mode;
     if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
     if (wtype < COUPE_INT || wtype > COUPE_DOUBLE) {
@@ -266,7 +272,8 @@ coupe_err device_call(bool rib, uint64_t *d_partition, uint64_t n, uint64_t dime
     int rc = COUPE_ERR_OK;
     if (rib) {
         double M[9];
-        rc = cg::rib_matrix(*C, n, (int)dimension, d_points, a.stream, M, &err);
+        rc = winert ? cg::rib_matrix(*C, n, (int)dimension, d_points, a.stream, M, &err, wtype, d_weights)
+                    : cg::rib_matrix(*C, n, (int)dimension, d_points, a.stream, M, &err);
         if (rc == COUPE_ERR_OK) {
             a.has_matrix = true;
             std::memcpy(a.matrix, M, sizeof(M));
@@ -424,6 +431,32 @@ enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double
     }
     std::lock_guard<std::mutex> lock(C->mu);
     int rc = cg::rib_matrix(*C, n, (int)dimension, d_points, (cudaStream_t)stream, obb_to_aabb, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+enum coupe_err coupe_gpu_rib_matrix_weighted(uint64_t n, uint64_t dimension, const double *d_points,
+                                             enum coupe_type weight_type, const void *d_weights, double *obb_to_aabb,
+                                             void *stream) {
+    t_err.clear();
+    if (dimension != 2 && dimension != 3) return COUPE_ERR_BAD_DIMENSION;
+    if (weight_type < COUPE_INT || weight_type > COUPE_DOUBLE) {
+        t_err = "unknown weight type";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (n == 0 || !d_weights) {
+        t_err = "no points";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    int rc = cg::rib_matrix(*C, n, (int)dimension, d_points, (cudaStream_t)stream, obb_to_aabb, &err, weight_type,
+                            d_weights);
     if (rc != COUPE_ERR_OK) t_err = err;
     return (coupe_err)rc;
 }

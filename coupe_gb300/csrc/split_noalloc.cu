@@ -293,6 +293,11 @@ int split_noalloc(uint64_t n, uint64_t dimension, const double *d_points, int we
         *msg = "NULL input or output pointer";
         return COUPE_ERR_BAD_TYPE;
     }
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        // not ours: an error the caller's earlier work left pending
+        *msg = "a CUDA error from earlier work on this thread is pending (cudaPeekAtLastError); nothing was launched";
+        return COUPE_ERR_CRASH;
+    }
     SplitDevice *S = nullptr;
     int rc = split_setup(&S, msg);
     if (rc != COUPE_ERR_OK) return rc;

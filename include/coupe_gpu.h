@@ -92,6 +92,14 @@ enum coupe_err coupe_gpu_rcb_batched(uint64_t *d_partition, uint64_t nsets,
 		enum coupe_type weight_type, const void *d_weights,
 		const uint32_t *iter_counts, double tolerance, int mode, void *stream);
 
+/* Flag OR'ed into the mode of coupe_gpu_rib / coupe_gpu_rib_device (no
+ * counterpart in the reference): the Rib inertia matrix weighs each point by
+ * its weight — centroid sum(w p) / sum(w), M = sum(w (p - c)(p - c)^T).
+ * coupe's inertia_matrix is unweighted (coupe/src/geometry.rs:273-284) and
+ * stays the default.  The weights must have a positive finite sum, else
+ * COUPE_ERR_BAD_TYPE. */
+#define COUPE_GPU_WEIGHTED_INERTIA 0x100
+
 /* Rib on device-resident inputs (see coupe_gpu_rcb_device). */
 enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
 		const double *d_points, enum coupe_type weight_type, const void *d_weights,
@@ -103,6 +111,12 @@ enum coupe_err coupe_gpu_rib_device(uint64_t *d_partition, uint64_t n, uint64_t 
  * (coupe/src/geometry.rs:210-228, 273-319). */
 enum coupe_err coupe_gpu_rib_matrix(uint64_t n, uint64_t dimension, const double *d_points,
 		double *obb_to_aabb, void *stream);
+
+/* The same with the weighted inertia matrix of COUPE_GPU_WEIGHTED_INERTIA
+ * (no counterpart in the reference): `d_weights` holds n device-resident
+ * elements of `weight_type`. */
+enum coupe_err coupe_gpu_rib_matrix_weighted(uint64_t n, uint64_t dimension, const double *d_points,
+		enum coupe_type weight_type, const void *d_weights, double *obb_to_aabb, void *stream);
 
 /* The engine's f64 -> f32 key conversion (coupe's `point[coord] as f32`,
  * coupe/src/algorithms/recursive_bisection.rs:677) applied to n device
@@ -208,7 +222,11 @@ enum coupe_err coupe_gpu_imbalance_device(uint64_t num_parts, const uint64_t *d_
  * The first call on each device (with that device current) does a one-time
  * set-up: it looks up the scratch's device address with
  * cudaGetSymbolAddress and sets the kernels' shared-memory limit.  Make that
- * first call before any stream capture. */
+ * first call before any stream capture.  The set-up is kept for the life of
+ * the process: after cudaDeviceReset on a device, this entry point must not
+ * be called on that device again.  A launch error left pending by the
+ * caller's own earlier work is reported as such (COUPE_ERR_CRASH) before any
+ * kernel of this call is launched. */
 enum coupe_err coupe_gpu_split_noalloc(uint64_t n, uint64_t dimension,
 		const double *d_points, enum coupe_type weight_type, const void *d_weights,
 		uint64_t coord, double cut, double *d_out_points, void *d_out_weights,
@@ -243,6 +261,14 @@ const char *coupe_gpu_kernel_name(int id);
  *                             every pass (by default the bins hold truncated
  *                             sums and a decision they cannot settle is
  *                             replayed from exact bins)
+ * and two failure-handling knobs:
+ *   "lookback_spin_limit"     polls of a reorder chunk's wait for its
+ *                             predecessor's prefix before the run fails with
+ *                             COUPE_ERR_CRASH (default 2^22; 0 makes every
+ *                             unfinished predecessor a failure)
+ *   "workspace_limit_mb"      cap on the engine's device workspace in MiB (0:
+ *                             none); a run needing more fails with
+ *                             COUPE_ERR_ALLOC before allocating
  * Returns COUPE_ERR_OK, or COUPE_ERR_BAD_TYPE for an unknown name. */
 int coupe_gpu_set_option(const char *name, int64_t value);
 

@@ -53,6 +53,8 @@ def lib():
         L.oracle_record_splits.argtypes = [vp, u64]
         L.oracle_record_splits.restype = None
         L.oracle_rib_matrix.argtypes = [u64, i32, vp, vp]
+        L.oracle_rib_matrix_weighted.argtypes = [u64, i32, vp, vp, vp]
+        L.oracle_rib_matrix_weighted.restype = i32
         L.oracle_rib_matrix.restype = i32
         L.oracle_map_points.argtypes = [vp, u64, i32, vp, vp]
         L.oracle_bbox.argtypes = [vp, u64, i32, vp, vp]
@@ -164,6 +166,19 @@ def rib_matrix(points):
     rc = lib().oracle_rib_matrix(n, dim, p.ctypes.data, m.ctypes.data)
     if rc != 0:
         raise ValueError("oracle_rib_matrix failed (%d)" % rc)
+    return m
+
+
+def rib_matrix_weighted(points, weights):
+    """The basis change of the weighted inertia matrix (the GPU library's
+    opt-in; coupe's own is unweighted)."""
+    p = np.ascontiguousarray(np.asarray(points, dtype=np.float64))
+    w = np.ascontiguousarray(np.asarray(weights, dtype=np.float64))
+    n, dim = p.shape
+    m = np.zeros((dim, dim))
+    rc = lib().oracle_rib_matrix_weighted(n, dim, p.ctypes.data, w.ctypes.data, m.ctypes.data)
+    if rc != 0:
+        raise ValueError("oracle_rib_matrix_weighted failed (%d)" % rc)
     return m
 
 

@@ -767,6 +767,31 @@ void oracle_record_splits(double *buf, uint64_t cap) {
     g_split_cap = buf ? cap : 0;
 }
 
+// The weighted variant of the basis change (the GPU library's opt-in, no
+// counterpart in coupe): centroid sum(w p) / sum(w), then sum(w (p-c)(p-c)^T),
+// both sequential, then the same eigenvector, Householder and inverse.
+int oracle_rib_matrix_weighted(uint64_t n, int dim, const double *pts, const double *w, double *obb_to_aabb) {
+    if (dim != 2 && dim != 3) return -1;
+    double c[3] = {0, 0, 0}, W = 0.0, m[9], v[3], h[9];
+    for (size_t i = 0; i < n; ++i) {
+        W += w[i];
+        for (int d = 0; d < dim; ++d) c[d] += w[i] * pts[i * dim + d];
+    }
+    if (!(W > 0.0)) return -3;
+    for (int d = 0; d < dim; ++d) c[d] = c[d] / W;
+    for (int k = 0; k < dim * dim; ++k) m[k] = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        double o[3];
+        for (int d = 0; d < dim; ++d) o[d] = pts[i * dim + d] - c[d];
+        for (int a = 0; a < dim; ++a)
+            for (int b = 0; b < dim; ++b) m[a * dim + b] += w[i] * o[a] * o[b];
+    }
+    inertia_vector(m, dim, v);
+    householder(v, dim, h);
+    if (!inverse(h, dim, obb_to_aabb)) return -2;
+    return 0;
+}
+
 // The Rib basis change (OrientedBoundingBox::from_points, geometry.rs:210-228):
 // writes obb_to_aabb (row-major dim x dim).
 int oracle_rib_matrix(uint64_t n, int dim, const double *pts, double *obb_to_aabb) {

@@ -108,3 +108,35 @@ def test_split_ragged_sizes_nan_and_signed_zero(coupe, n):
         assert np.array_equal(op, want_p, equal_nan=True)
         assert np.array_equal(np.signbit(op), np.signbit(want_p))
         assert np.array_equal(ow, np.concatenate([w[mask], w[~mask]]))
+
+
+@pytest.mark.gpu
+def test_split_allocates_nothing(coupe):
+    """After the first call's set-up, a call changes neither the device's free
+    memory (cudaMemGetInfo) nor torch's allocator: the outputs are the
+    caller's and the scratch is the library's static array."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    n = 2_000_000
+    dp = torch.from_numpy(rng.random((n, 3))).cuda()
+    dw = torch.from_numpy(rng.integers(1, 9, n).astype(np.int64)).cuda()
+    op = torch.empty_like(dp)
+    ow = torch.empty_like(dw)
+    f = _split(coupe)
+    nl = ctypes.c_uint64(0)
+    s = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        return f(n, 3, dp.data_ptr(), coupe.COUPE_INT64, dw.data_ptr(), 1, 0.5, op.data_ptr(), ow.data_ptr(),
+                 ctypes.byref(nl), s)
+    assert call() == ERR_OK  # set-up on this device (if not done already)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+    for _ in range(3):
+        assert call() == ERR_OK
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_allocated() == alloc0 and torch.cuda.memory_reserved() == reserved0
+    assert nl.value == int((dp[:, 1] < 0.5).sum().item())
