@@ -143,6 +143,13 @@ def cpu_baseline(pts, w, cfg, budget_s=20.0):
                       "Rcb (reference is Rust, not buildable here)" % (len(pts), len(times), t)}, ids
 
 
+def _headline_config(cfg, n, input_bytes):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": cfg["name"], "points": n, "dim": 3, "parts": 1 << cfg["iter_count"],
+            "iter_count": cfg["iter_count"], "tolerance": cfg["tolerance"], "weights": "int64 U{1..100}",
+            "l2": "inputs larger than L2 (%d MB per step), no flush" % (input_bytes >> 20)}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -175,8 +182,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["name"], "points": n, "dim": 3, "parts": 1 << cfg["iter_count"],
-                   "iter_count": cfg["iter_count"], "tolerance": cfg["tolerance"], "weights": "int64 U{1..100}"},
+        "config": _headline_config(cfg, n, pts.nbytes + w.nbytes),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d of %d points per step (first points of the seeded workload); OpenMP "
                                    "restatement of coupe Rcb on all host cores" % (sample, n)},
@@ -382,10 +388,8 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if headline == "f32key_f64band" else "f32",
         "data": "synthetic",
-        "config": {"workload": cfg["name"], "points": n, "dim": 3, "parts": 1 << iters, "iter_count": iters,
-                   "tolerance": tol, "weights": "int64 U{1..100}", "mode": headline,
-                   "l2": "inputs larger than L2 (%d MB per step), no flush" % ((pts_h.nbytes + w_h.nbytes) >> 20),
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "config": _headline_config(cfg, n, pts_h.nbytes + w_h.nbytes),
+        "mode": headline, "parallelism": "replicas" if world > 1 else "single",
         "modes": {m: {"ms_per_step": round(results[m], 4), "value": round(world * n / (results[m] / 1e3) / 1e6, 2)}
                   for m in results},
         "e2e": {"value": round(world * n / t_e2e / 1e6, 2), "unit": UNIT,

@@ -61,7 +61,7 @@ class Stats(ctypes.Structure):
         "hist_points", "band_points", "kernel_launches", "algo_bytes")] + [
         ("root_weight_sum", ctypes.c_double), ("device_ms", ctypes.c_double),
         ("fixed_scale", ctypes.c_int), ("mode", ctypes.c_int), ("weight_rechecks", ctypes.c_uint64),
-        ("weight_sum_error_bound", ctypes.c_double)]
+        ("weight_sum_error_bound", ctypes.c_double), ("host_syncs", ctypes.c_uint64)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

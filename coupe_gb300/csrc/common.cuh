@@ -556,7 +556,11 @@ struct RunScalars {
     uint32_t fapprox;                // f64 weights: bins hold approximate weights (see k_hist)
     uint32_t nexactw;                // decisions that needed exact f64 weight sums
     uint32_t decide_done;            // CTAs of the running k_decide that finished (reset by the last)
-    uint32_t pad3;
+    uint32_t stall;                  // queued run: level + 1 whose splits need more passes than queued
 };
+
+// A queued kernel has nothing to do after a device check failed or a split
+// needed more passes than were queued (the host finishes the run).
+__host__ __device__ __forceinline__ bool run_halted(const RunScalars *rs) { return (rs->err | rs->stall) != 0; }
 
 }  // namespace cg

@@ -55,6 +55,11 @@ struct Tuning {
     // COUPE_ERR_ALLOC before allocating, as an out-of-memory device would).
     int lookback_spin_limit = 1 << 22;
     int workspace_limit_mb = 0;
+    // 1: wait for every level's decisions before queuing the next (the host
+    // synchronises once per level); 0: queue the whole run and synchronise
+    // once, finishing level by level only after a split needed a third pass.
+    // The ids are the same.
+    int sync_levels = 0;
 };
 Tuning &tuning();
 

@@ -812,6 +812,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "exact_f64_hist")) return &t.exact_f64_hist;
     if (!std::strcmp(name, "lookback_spin_limit")) return &t.lookback_spin_limit;
     if (!std::strcmp(name, "workspace_limit_mb")) return &t.workspace_limit_mb;
+    if (!std::strcmp(name, "sync_levels")) return &t.sync_levels;
     return nullptr;
 }
 

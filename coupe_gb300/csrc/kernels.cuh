@@ -193,6 +193,15 @@ __device__ __forceinline__ CtaRange cta_tiles(uint64_t ntiles, uint32_t b, uint3
     return CtaRange{ntiles * b / g, ntiles * (b + 1) / g};
 }
 
+// run_halted read once per CTA (thread 0, then a barrier), so that every
+// thread of the CTA takes the same branch around the barriers that follow.
+__device__ __forceinline__ bool cta_halted(const RunScalars *rs) {
+    __shared__ int s_halt;
+    if (threadIdx.x == 0) s_halt = run_halted(rs) ? 1 : 0;
+    __syncthreads();
+    return s_halt != 0;
+}
+
 __device__ __forceinline__ void atomic_max_ord(uint32_t *p, uint32_t v) { atomicMax(p, v); }
 
 // 64-bit add to shared memory from 32-bit atomics: sm_103 has no 64-bit
@@ -591,7 +600,10 @@ __device__ Seg<KT> root_seg(uint64_t off, uint64_t voff, uint64_t n, uint32_t se
 
 // Root segment of a one-set run.
 template <class KT, class WT>
-__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs, int approx) {
+__global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, int D, RunScalars *rs, int approx,
+                       uint64_t *lvl) {
+    lvl[0] = 1;  // level 0: one segment of n items
+    lvl[1] = n;
     const int fs = WT::LIMBS > 1 ? run_fscale(rs, n) : 0;
     rs->fscale = fs;
     rs->qb = approx_shift(n);
@@ -608,9 +620,13 @@ __global__ void k_root(Seg<KT> *segs, uint32_t *list, uint64_t *P, uint64_t n, i
 // P[r] in the level's list of items (P written by the host).
 template <class KT, class WT>
 __global__ void k_roots(Seg<KT> *segs, uint32_t *list, const uint64_t *P, const uint32_t *roots, uint32_t nroots,
-                        int D, SetTab sets, RunScalars *rs, int approx) {
+                        int D, SetTab sets, RunScalars *rs, int approx, uint64_t *lvl) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r == 0) rs->fapprox = WT::LIMBS > 1 && approx && rs->fneg == 0;
+    if (r == 0) {
+        rs->fapprox = WT::LIMBS > 1 && approx && rs->fneg == 0;
+        lvl[0] = nroots;  // level 0: the root segments and their items
+        lvl[1] = P[nroots];
+    }
     if (r >= nroots) return;
     const uint32_t st = roots[r];
     const int fs = WT::LIMBS > 1 ? sets.fs[st] : 0;
@@ -906,7 +922,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                                                 const uint64_t *__restrict__ P, uint32_t nlist,
                                                 const typename KT::T *__restrict__ keys,
                                                 const typename WT::S *__restrict__ wts, Hist<KT, WT> H, int nbk,
-                                                uint64_t n_total, const RunScalars *rs, int nlist_dev,
+                                                uint64_t n_total, const RunScalars *rs, const uint64_t *nlist_ptr,
                                                 const uint32_t *__restrict__ isrc, BandSrc bs, int coord,
                                                 Seg<KT> *segs_w, const int32_t *__restrict__ set_fs,
                                                 const int32_t *__restrict__ set_qb) {
@@ -941,7 +957,10 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
     int qb = L > 1 ? rs->qb : 0;      // several sets: each set's own (set_qb)
     const bool packed_all = L == 1 && rs->wide == 0;
     const bool fapprox = L > 1 && rs->fapprox != 0;
-    if (nlist_dev) nlist = (uint32_t)rs->nactive;  // a speculative pass: the list the last scan left
+    if (cta_halted(rs)) return;
+    // the list's length from the device (a speculative pass: the list the
+    // last scan left; a queued level: its segment count)
+    if (nlist_ptr) nlist = (uint32_t)*nlist_ptr;
     const uint64_t T = P[nlist];
     const uint64_t c0 = T * blockIdx.x / gridDim.x, c1 = T * (blockIdx.x + 1) / gridDim.x;
     if (c0 >= c1) return;
@@ -1486,12 +1505,13 @@ template <class KT, class WT>
 __device__ __forceinline__ void children_body(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
                                               uint32_t level, Seg<KT> *next, uint32_t *next_list, uint64_t *next_P,
                                               Trav<KT> *trav, RunScalars *rs, const SetTab &sets, int phase,
-                                              uint64_t *blk) {
+                                              uint64_t *blk, const uint64_t *S_ptr, uint64_t *lvl) {
     typedef typename KT::T K;
     __shared__ uint64_t sh[33];
     // launched right after a speculative pass: nothing to do while a segment
     // of the level is still searching (the host runs more passes, then this)
-    if (rs->nactive != 0) return;
+    if (cta_halted(rs) || rs->nactive != 0) return;
+    if (S_ptr) S = (uint32_t)*S_ptr;  // the level's segment count from the device
     const bool multi = sets.count > 1;
     uint64_t outc = 0, outv = 0;
     uint64_t hmin = ~0ull;
@@ -1527,6 +1547,10 @@ __device__ __forceinline__ void children_body(Seg<KT> *segs, uint32_t S, int coo
         if (threadIdx.x == 0) {
             rs->nsegs_next = outc;
             rs->items_next = outv;
+            if (lvl) {
+                lvl[2 * (level + 1)] = outc;  // the next level's counts
+                lvl[2 * (level + 1) + 1] = outv;
+            }
             if (write) next_P[outc] = outv;
         }
         return;
@@ -1645,6 +1669,10 @@ __device__ __forceinline__ void children_body(Seg<KT> *segs, uint32_t S, int coo
     if (phase == CHILD_ALL && threadIdx.x == 0) {
         rs->nsegs_next = outc;
         rs->items_next = outv;
+        if (lvl) {
+            lvl[2 * (level + 1)] = outc;  // the next level's counts
+            lvl[2 * (level + 1) + 1] = outv;
+        }
         if (write) next_P[outc] = outv;
     }
 }
@@ -1653,8 +1681,9 @@ template <class KT, class WT>
 __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, int coord, int D, int write,
                                                    uint32_t level, Seg<KT> *next, uint32_t *next_list,
                                                    uint64_t *next_P, Trav<KT> *trav, RunScalars *rs, SetTab sets,
-                                                   int phase, uint64_t *blk) {
-    children_body<KT, WT>(segs, S, coord, D, write, level, next, next_list, next_P, trav, rs, sets, phase, blk);
+                                                   int phase, uint64_t *blk, const uint64_t *S_ptr, uint64_t *lvl) {
+    children_body<KT, WT>(segs, S, coord, D, write, level, next, next_list, next_P, trav, rs, sets, phase, blk,
+                          S_ptr, lvl);
 }
 
 // The next level's segments built by the last CTA of a decide launch (levels
@@ -1662,6 +1691,9 @@ __global__ void __launch_bounds__(1024) k_children(Seg<KT> *segs, uint32_t S, in
 template <class KT>
 struct ChildArgs {
     int on;
+    uint32_t stall_level;  // nonzero: halt the queued run with this value if splits still search
+    const uint64_t *S_ptr;  // the level's segment count on the device (NULL: S)
+    uint64_t *lvl;          // per-level segment and item counts (the children write the next level's)
     uint32_t S;
     int coord, D, write;
     uint32_t level;
@@ -1744,8 +1776,39 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
 #pragma unroll
     for (int l = 0; l < L; ++l) Tw[l] = 0;
     if (lane * BS < NB) {
-        // four bins per step, their loads in flight together
         int j = 0;
+        {
+            // eight bins per step in 16-byte loads, all in flight together
+            // (a lane's block of bins is contiguous and 16-byte aligned)
+            constexpr int MV = 8 * sizeof(O) / 16;  // 16-byte vectors of minima per step
+            for (; j + 8 <= BS; j += 8) {
+                const size_t g = g0 + lane * BS + j;
+                uint4 c4[2], m4[MV];
+                ulonglong2 w2[4 * L];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) c4[q] = *(const uint4 *)&H.cnt[g + 4 * q];
+#pragma unroll
+                for (int q = 0; q < MV; ++q) m4[q] = *(const uint4 *)((const char *)&H.inv[g] + 16 * q);
+#pragma unroll
+                for (int q = 0; q < 4 * L; ++q) w2[q] = *(const ulonglong2 *)&H.w[g * L + 2 * q];
+#pragma unroll
+                for (int q = 0; q < 2; ++q) Tc += (uint64_t)c4[q].x + c4[q].y + c4[q].z + c4[q].w;
+                const O *mo = (const O *)m4;
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    O o = (O)~mo[r];  // empty bins hold 0: ~0
+                    if (!KT::BAND) o = o > KT::ORD_INF ? KT::ORD_INF : o;
+                    Tm = o < Tm ? o : Tm;
+                }
+#pragma unroll
+                for (int q = 0; q < 4 * L; ++q) {
+                    // element 2q + h of the step is limb (2q + h) % L of a bin
+                    Tw[(2 * q) % L] += w2[q].x;
+                    Tw[(2 * q + 1) % L] += w2[q].y;
+                }
+            }
+        }
+        // four bins per step, their loads in flight together
         for (; j + 4 <= BS; j += 4) {
             uint64_t c[4], w[4][L];
             O m[4];
@@ -2056,13 +2119,15 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
 template <class KT, class WT>
 __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t *__restrict__ list, uint32_t nlist,
                                                   Hist<KT, WT> H, int nbk, double tol, uint32_t *flags,
-                                                  RunScalars *rs, int nlist_dev, const int32_t *__restrict__ set_fs,
+                                                  RunScalars *rs, const uint64_t *nlist_ptr,
+                                                  const int32_t *__restrict__ set_fs,
                                                   const int32_t *__restrict__ set_qb, uint32_t *list2, uint64_t *P2,
                                                   ChildArgs<KT> ca) {
     __shared__ uint32_t s_last;
-    // a speculative pass: the list the last scan left (the grid is an upper
-    // bound); every CTA reads it before the last one overwrites it
-    if (nlist_dev) nlist = (uint32_t)rs->nactive;
+    if (cta_halted(rs)) return;
+    // the list's length from the device (the grid is an upper bound); every
+    // CTA reads it before the last one's scan overwrites it
+    if (nlist_ptr) nlist = (uint32_t)*nlist_ptr;
     const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
     if (k < nlist) decide_one<KT, WT>(segs, list, k, H, nbk, tol, flags, rs, set_fs, set_qb);
     __threadfence();
@@ -2072,11 +2137,16 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
     if (s_last) {
         __threadfence();
         scan_list_block<KT>(segs, list, flags, nlist, list2, P2, rs);
-        if (threadIdx.x == 0) rs->decide_done = 0;
+        if (threadIdx.x == 0) {
+            rs->decide_done = 0;
+            // a queued level's last queued pass: splits still searching halt
+            // the queued kernels after it (the host runs more passes)
+            if (ca.stall_level && rs->nactive != 0) rs->stall = ca.stall_level;
+        }
         if (ca.on) {
             __syncthreads();  // the scan's count (rs->nactive) is read below
             children_body<KT, WT>(segs, ca.S, ca.coord, ca.D, ca.write, ca.level, ca.next, ca.next_list, ca.next_P,
-                                  ca.trav, rs, ca.sets, CHILD_ALL, nullptr);
+                                  ca.trav, rs, ca.sets, CHILD_ALL, nullptr, ca.S_ptr, ca.lvl);
         }
     }
 }
@@ -2112,6 +2182,8 @@ struct ReorderArgs {
     RunScalars *rs;
     BandSrc bs;    // band form: the f64 coordinates (through isrc)
     uint32_t spin_limit;  // polls of a look-back wait before it fails (ERR_LOOKBACK_TIMEOUT)
+    const uint64_t *S_ptr;  // the level's segment and item counts on the device (NULL: S, n)
+    const uint64_t *n_ptr;
 };
 
 // One tile in shared memory: D key arrays and a weight array, each with 16
@@ -2236,16 +2308,24 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         cp_async_commit();
     };
 
+    if (cta_halted(A.rs)) return;
+    // the level's counts from the device when the host queued the level
+    // without them (chunks of the host's size over the actual items); kept
+    // in locals: writing to the parameter struct would copy it to local
+    // memory
+    const uint32_t A_S = A.S_ptr ? (uint32_t)*A.S_ptr : A.S;
+    const uint64_t A_n = A.n_ptr ? *A.n_ptr : A.n;
+    const uint64_t A_nchunks = A.n_ptr ? (A_n + A.chunk - 1) / A.chunk : A.nchunks;
     for (;;) {
         if (threadIdx.x == 0) s_ticket = atomicAdd((unsigned long long *)&A.rs->ticket, 1ull);
         __syncthreads();
         const uint64_t t = s_ticket;
-        if (t >= A.nchunks) break;
+        if (t >= A_nchunks) break;
         // [c0, c1): positions in the list of the level's items; a segment's
         // items are at off + (position - voff)
-        const uint64_t c0 = t * A.chunk, c1 = min(A.n, c0 + A.chunk);
-        const uint32_t kf = seg_index_of_v<KT>(A.segs, A.S, c0);
-        const uint32_t kl = seg_index_of_v<KT>(A.segs, A.S, c1 - 1);
+        const uint64_t c0 = t * A.chunk, c1 = min(A_n, c0 + A.chunk);
+        const uint32_t kf = seg_index_of_v<KT>(A.segs, A_S, c0);
+        const uint32_t kl = seg_index_of_v<KT>(A.segs, A_S, c1 - 1);
         auto piece_end = [&](const Seg<KT> &g) { return g.off + (min(c1, g.voff + g.n) - g.voff); };
         const Seg<KT> sf = A.segs[kf];
         TileRef cur;
@@ -2483,6 +2563,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse(const Trav<KT> *__restrict__
                                                     uint64_t *__restrict__ part, const RunScalars *rs, BandSrc bs) {
     typedef typename KT::T K;
     constexpr int CAP = TRAV_SMEM_BYTES / sizeof(Trav<KT>);
+    if (cta_halted(rs)) return;
     __shared__ Trav<KT> st[CAP];
     const uint64_t cached = trav_total < (uint64_t)CAP ? trav_total : (uint64_t)CAP;
     for (uint64_t j = threadIdx.x; j < cached; j += BLOCK) st[j] = trav[j];
@@ -2547,6 +2628,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_smem(const Trav<KT> *__restr
                                                          BandSrc bs) {
     typedef typename KT::T K;
     typedef typename KT::C CK;
+    if (cta_halted(rs)) return;
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ uint32_t s_off[MAX_TRAV_LEVELS];
     const uint32_t off_last = (uint32_t)lv.off[levels - 1];
@@ -2661,6 +2743,7 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_band(const Trav<KeyBand> *__
                                                          const RunScalars *rs, BandSrc bs) {
     extern __shared__ __align__(16) unsigned char dsm[];
     __shared__ uint32_t s_off[MAX_TRAV_LEVELS];
+    if (cta_halted(rs)) return;
     const uint32_t off_last = (uint32_t)lv.off[levels - 1];
     BandNode *s_node = (BandNode *)dsm;                   // [total]
     uint64_t *s_heap = (uint64_t *)(s_node + total);      // [total - off_last]
@@ -2760,9 +2843,11 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_sets(const Trav<KT> *__restr
                                                          const typename KT::T *__restrict__ k0,
                                                          const typename KT::T *__restrict__ k1,
                                                          const typename KT::T *__restrict__ k2, uint64_t n,
-                                                         uint64_t *__restrict__ part, SetTab sets, BandSrc bs) {
+                                                         uint64_t *__restrict__ part, SetTab sets, BandSrc bs,
+                                                         const RunScalars *rs) {
     typedef typename KT::T K;
     constexpr uint64_t TILE = (uint64_t)BLOCK * TRAV_ILP;
+    if (cta_halted(rs)) return;
     const CtaRange r = cta_tiles((n + TILE - 1) / TILE, blockIdx.x, gridDim.x);
     SetCursor cur;
     for (uint64_t t = r.t0; t < r.t1; ++t) {
@@ -2832,7 +2917,10 @@ __global__ void __launch_bounds__(BLOCK) k_traverse_sets(const Trav<KT> *__restr
 template <class KT>
 __global__ void __launch_bounds__(BLOCK) k_assign(const Seg<KT> *__restrict__ segs, uint32_t S, uint64_t n,
                                                   const typename KT::T *__restrict__ kc, const uint32_t *__restrict__ isrc,
-                                                  uint64_t *__restrict__ part, RunScalars *rs, BandSrc bs, int coord) {
+                                                  uint64_t *__restrict__ part, RunScalars *rs, BandSrc bs, int coord,
+                                                  const uint64_t *S_ptr) {
+    if (cta_halted(rs)) return;
+    if (S_ptr) S = (uint32_t)*S_ptr;
     const uint64_t c0 = n * blockIdx.x / gridDim.x, c1 = n * (blockIdx.x + 1) / gridDim.x;
     if (c0 >= c1) return;
     const uint64_t hmin = rs->min_heap;

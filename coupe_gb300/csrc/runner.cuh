@@ -6,14 +6,32 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
+
+#include <nvtx3/nvToolsExt.h>
 
 #include "engine.h"
 #include "kernels.cuh"
 
 namespace cg {
+
+// NVTX range over a scope (a run, a tree level, an extra pass): the GPU
+// counterpart of coupe's tracing spans (recursive_bisection.rs:467-468,
+// 590-595).  Visible in Nsight timelines; a no-op without a tool attached.
+struct NvtxScope {
+    explicit NvtxScope(const char *name) { nvtxRangePushA(name); }
+    NvtxScope(const char *what, uint64_t k) {
+        char b[48];
+        snprintf(b, sizeof(b), "%s %llu", what, (unsigned long long)k);
+        nvtxRangePushA(b);
+    }
+    ~NvtxScope() { nvtxRangePop(); }
+    NvtxScope(const NvtxScope &) = delete;
+    NvtxScope &operator=(const NvtxScope &) = delete;
+};
 
 #define CG_CK(call)                                               \
     do {                                                          \
@@ -61,6 +79,7 @@ struct Buffers {
     uint64_t *lb;
     uint64_t *blk;   // per-CTA child counts of the grid form of k_children
     Trav<KT> *trav;  // finished splits of every level (traversal path only)
+    uint64_t *lvl;   // [2 (levels + 1)]: segments and items of each level
     RunScalars *rs;
     uint64_t hist_bins;
     // several sets: the set table and the sets of the root segments
@@ -85,7 +104,7 @@ struct Buffers {
     }
 
     size_t carve(Bump &b, uint64_t n, uint64_t scap, uint64_t hb, uint64_t lbcap, bool index_path, bool carry,
-                 uint64_t tcap, uint64_t nsets = 0) {
+                 uint64_t tcap, uint64_t nsets, uint64_t levels) {
         for (int k = 0; k < 3; ++k)
             for (int d = 0; d < 3; ++d) keys[k][d] = d < D ? b.take<K>(n) : nullptr;
         for (int s = 0; s < 2; ++s) {
@@ -102,6 +121,7 @@ struct Buffers {
         lb = b.take<uint64_t>(lbcap);
         blk = b.take<uint64_t>(2 * (scap / 1024 + 1));
         trav = index_path ? nullptr : b.take<Trav<KT>>(tcap);
+        lvl = b.take<uint64_t>(2 * (levels + 1));
         rs = b.take<RunScalars>(1);
         hist_bins = hb;
         set_off = set_bmin = set_bmax = set_wsum = set_wabs = set_minheap = nullptr;
@@ -142,6 +162,7 @@ struct RunSetup {
     cudaStream_t s = nullptr;
     RunScalars *h_rs = nullptr;
     int g_stream = 0;
+    std::vector<uint64_t> smax, vmax;  // per level: most segments, and items
 };
 
 // The level loop of one run; WT is the caller's weight type (it sizes the
@@ -187,156 +208,196 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     if (multi) {
         CG_LAUNCH(KID_ROOT, 0,
                   k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,
-                                                                           R0.nroots, D, sets, B.rs, approx));
+                                                                           R0.nroots, D, sets, B.rs, approx,
+                                                                           B.lvl));
     } else {
-        CG_LAUNCH(KID_ROOT, 0, k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs, approx));
+        CG_LAUNCH(KID_ROOT, 0,
+                  k_root<KT, WL><<<1, 1, 0, s>>>(B.segs[0], B.list[0], B.P[0], n, D, B.rs, approx, B.lvl));
     }
     const uint64_t sk = sizeof(K), sw = sizeof(WS), si = carry ? 4 : 0;
 
-    int kb = 0;          // key buffer of the current level
-    int sb = 0;          // segment table / weight buffer of the current level
-    bool level0 = true;  // level 0 reads the caller's weights and implicit indices
-    uint64_t S = R0.nroots;
-    uint64_t V = R0.v0;  // items of the level's segments
+    // Per-level bounds known on the host: segments S_max (a level holds at
+    // most min(2^L, n_k) segments of each set still splitting) and items V
+    // (every item of a set still splitting is in one of its segments).  The
+    // level's kernels read the actual counts from the device
+    // (Buffers::lvl, written by the root kernel and by each level's
+    // children), so the host queues a whole run
+    // without waiting: grids, bins and recorded-split offsets are sized by
+    // S_max.  A split that needs more passes than the two queued per level
+    // halts the queued kernels after it (RunScalars::stall); the host then
+    // finishes that level with more passes and continues level by level,
+    // waiting for each (the option sync_levels forces that from the start).
+    const std::vector<uint64_t> &smax = R0.smax, &vmax = R0.vmax;
     LevelOffsets lv;
     uint64_t trav_used = 0;
+    for (uint64_t L = 0; L < iters; ++L) {
+        lv.off[L < (uint64_t)MAX_TRAV_LEVELS ? L : 0] = index_path ? 0 : trav_used;
+        if (!index_path) trav_used += smax[L];
+    }
     // bins per segment: as many bisection steps per pass as the budget allows
     auto pick_nbk = [&](uint64_t nseg) {
         int k = nbk_max;
         while (k > 1 && nseg * (1ull << k) > B.hist_bins) --k;
         return k;
     };
-    int nbk = pick_nbk(S);
     int err_level = -1;  // level at whose synchronisation a device check was first seen
     Hist<KT, WL> H{B.hcnt, B.hw, B.hinv};
-    for (uint64_t L = 0; L < iters; ++L) {
+    // buffers of level L: segment tables and weights alternate; keys are the
+    // kept level-0 copy on level 0, then the two reorder buffers in turn
+    auto key_buf = [](uint64_t L) { return L == 0 ? 0 : (L % 2 == 1 ? 1 : 2); };
+    auto seg_buf = [](uint64_t L) { return (int)(L & 1); };
+
+    // Queues level L.  sync: wait for its decisions and run further passes
+    // while splits still search; resume: its two queued passes already ran
+    // (a halted queued run), so start with the further passes.
+    // speculative passes queued after each level's first one (1; one more
+    // for the levels queued again after a halt), and per level the list
+    // that holds the segments still searching after them
+    int nspec = 1;
+    std::vector<int> active_list(iters, 0);
+    auto level = [&](uint64_t L, bool sync, bool resume) -> int {
+        NvtxScope level_range("rcb level", L);
         const int coord = (int)(L % D);
+        const uint64_t S_max = smax[L], V = vmax[L];
+        const int nbk = pick_nbk(S_max);
         const uint64_t NB = 1ull << nbk;
+        const int kb = key_buf(L), sb = seg_buf(L);
+        const bool level0 = L == 0;  // level 0 reads the caller's weights and implicit indices
         const K *kc = B.keys[kb][coord];
         const WS *wc = level0 ? w_in : (const WS *)B.w[sb];
         const uint32_t *ic = level0 ? nullptr : B.idx[sb];
         Seg<KT> *segs = B.segs[sb];
         const bool last = L + 1 == iters;
         const int snext = sb ^ 1;
-        Trav<KT> *trav_l = nullptr;
-        if (!index_path) {
-            lv.off[L] = trav_used;
-            trav_l = B.trav + trav_used;
-            trav_used += S;
-        }
+        Trav<KT> *trav_l = index_path ? nullptr : B.trav + lv.off[L];
+        const uint64_t *S_dev = &B.lvl[2 * L];
+        const uint64_t *V_dev = &B.lvl[2 * L + 1];
         // band form: the items' input indices, for coordinates in the band
         const uint32_t *hsrc = KT::BAND ? ic : nullptr;
+        const bool fuse = S_max < CHILD_GRID_MIN;
         auto children = [&]() {
             const int wr = last ? 0 : 1;
-            if (S < CHILD_GRID_MIN) {
+            if (fuse) {
                 CG_LAUNCH(KID_CHILDREN, 0,
-                          k_children<KT, WL><<<1, 1024, 0, s>>>(segs, (uint32_t)S, coord, D, wr, (uint32_t)L,
-                                                                B.segs[snext], B.list[0], B.P[0], trav_l, B.rs, sets,
-                                                                CHILD_ALL, B.blk));
+                          k_children<KT, WL><<<1, 1024, 0, s>>>(segs, 0u, coord, D, wr, (uint32_t)L, B.segs[snext],
+                                                                B.list[0], B.P[0], trav_l, B.rs, sets, CHILD_ALL,
+                                                                B.blk, S_dev, B.lvl));
                 return (int)COUPE_ERR_OK;
             }
-            const unsigned g = (unsigned)((S + 1023) / 1024);
+            const unsigned g = (unsigned)((S_max + 1023) / 1024);
             for (int ph : {(int)CHILD_COUNT, (int)CHILD_SCAN, (int)CHILD_WRITE}) {
                 CG_LAUNCH(KID_CHILDREN, 0,
                           k_children<KT, WL><<<ph == CHILD_SCAN ? 1u : g, 1024, 0, s>>>(
-                              segs, (uint32_t)S, coord, D, wr, (uint32_t)L, B.segs[snext], B.list[0], B.P[0], trav_l,
-                              B.rs, sets, ph, B.blk));
+                              segs, 0u, coord, D, wr, (uint32_t)L, B.segs[snext], B.list[0], B.P[0], trav_l, B.rs,
+                              sets, ph, B.blk, S_dev, B.lvl));
             }
             return (int)COUPE_ERR_OK;
         };
-        const unsigned decide_grid = (unsigned)((S + NWARPS - 1) / NWARPS);
-        // levels below CHILD_GRID_MIN segments build their children in the
-        // last CTA of the speculative decide (when no segment is searching)
-        const bool fuse = S < CHILD_GRID_MIN;
+        const unsigned decide_grid = (unsigned)((S_max + NWARPS - 1) / NWARPS);
         ChildArgs<KT> no_ch;
         std::memset(&no_ch, 0, sizeof(no_ch));
-        ChildArgs<KT> ch = no_ch;
-        ch.on = fuse ? 1 : 0;
-        ch.S = (uint32_t)S;
-        ch.coord = coord;
-        ch.D = D;
-        ch.write = last ? 0 : 1;
-        ch.level = (uint32_t)L;
-        ch.next = B.segs[snext];
-        ch.next_list = B.list[0];
-        ch.next_P = B.P[0];
-        ch.trav = trav_l;
-        ch.sets = sets;
-        const uint64_t decide_bytes = S * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord));
-        // First pass over every point of the level, its decisions, and the
-        // list of segments still searching (list[1]).
-        CG_CK(cudaMemsetAsync(B.hcnt, 0, S * NB * sizeof(uint32_t), s));
-        CG_CK(cudaMemsetAsync(B.hw, 0, S * NB * WL::LIMBS * sizeof(uint64_t), s));
-        CG_CK(cudaMemsetAsync(B.hinv, 0, S * NB * sizeof(typename KT::Ord), s));
-        CG_LAUNCH(KID_HIST, V * (sk + sw),
-                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], (uint32_t)S, kc, wc, H, nbk, n,
-                                                          B.rs, 0, hsrc, bs, coord, segs, set_fs, set_qb));
-        ++st->hist_passes;
-        st->hist_points += V;
-        bytes += V * (sk + sw);
-        CG_LAUNCH(KID_DECIDE, decide_bytes,
-                  k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], (uint32_t)S, H, nbk, a.tolerance,
-                                                                 B.flags, B.rs, 0, set_fs, set_qb, B.list[1], B.P[1],
-                                                                 no_ch));
-        // A speculative second pass over list[1] without asking the host how
-        // long it is: its kernels read the count the scan left and return at
-        // once when no segment is searching.  The next scan leaves list[0].
-        CG_LAUNCH(KID_HIST, 0,
-                  k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[1], B.P[1], 0, kc, wc, H, nbk, n, B.rs, 1, hsrc,
-                                                          bs, coord, segs, set_fs, set_qb));
-        ++st->hist_passes;
-        CG_LAUNCH(KID_DECIDE, decide_bytes,
-                  k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[1], 0, H, nbk, a.tolerance, B.flags,
-                                                                 B.rs, 1, set_fs, set_qb, B.list[0], B.P[0], ch));
-        // k_children returns at once if a segment is still searching
-        if (!last && !fuse) {
-            const int rc_ = children();
-            if (rc_ != COUPE_ERR_OK) return rc_;
-        }
-        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
-        CG_CK(cudaStreamSynchronize(s));
-        if (h_rs->err) {
-            err_level = (int)L;
-            break;
-        }
-        // rare: splits that need more steps than two passes replay
-        int li = 0;
-        bool more = false;
-        int extra = 0;
-        while (h_rs->nactive > 0) {
-            more = true;
-            if (++extra > 4096) {
-                *err = "a split did not finish after 4096 passes";
-                return COUPE_ERR_CRASH;
-            }
-            const uint64_t nlist = h_rs->nactive;
-            CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
-                      k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc, H,
-                                                              nbk, n, B.rs, 0, hsrc, bs, coord, segs, set_fs, set_qb));
+        const uint64_t decide_bytes = S_max * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord));
+        if (!resume) {
+            // levels below CHILD_GRID_MIN segments build their children in
+            // the last CTA of the speculative decide (when no segment is
+            // searching any more)
+            ChildArgs<KT> ch = no_ch;
+            ch.on = fuse ? 1 : 0;
+            ch.stall_level = sync ? 0u : (uint32_t)(L + 1);
+            ch.S_ptr = S_dev;
+            ch.lvl = B.lvl;
+            ch.coord = coord;
+            ch.D = D;
+            ch.write = last ? 0 : 1;
+            ch.level = (uint32_t)L;
+            ch.next = B.segs[snext];
+            ch.next_list = B.list[0];
+            ch.next_P = B.P[0];
+            ch.trav = trav_l;
+            ch.sets = sets;
+            // First pass over every point of the level, its decisions, and
+            // the list of segments still searching (list[1]).
+            CG_CK(cudaMemsetAsync(B.hcnt, 0, S_max * NB * sizeof(uint32_t), s));
+            CG_CK(cudaMemsetAsync(B.hw, 0, S_max * NB * WL::LIMBS * sizeof(uint64_t), s));
+            CG_CK(cudaMemsetAsync(B.hinv, 0, S_max * NB * sizeof(typename KT::Ord), s));
+            CG_LAUNCH(KID_HIST, V * (sk + sw),
+                      k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[0], B.P[0], 0u, kc, wc, H, nbk, n, B.rs,
+                                                              S_dev, hsrc, bs, coord, segs, set_fs, set_qb));
             ++st->hist_passes;
-            CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
-                      k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
-                          segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, 0, set_fs, set_qb,
-                          B.list[li ^ 1], B.P[li ^ 1], no_ch));
-            li ^= 1;
+            st->hist_points += V;
+            bytes += V * (sk + sw);
+            CG_LAUNCH(KID_DECIDE, decide_bytes,
+                      k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], 0u, H, nbk, a.tolerance,
+                                                                     B.flags, B.rs, S_dev, set_fs, set_qb, B.list[1],
+                                                                     B.P[1], no_ch));
+            // Speculative passes over the list the last scan left: their
+            // kernels read its count and return at once when no segment is
+            // searching.  The lists alternate; the last pass's decide builds
+            // the children (next level's list in list[0], written only when
+            // its own scan, into the other list, found nothing searching).
+            const int ns = sync ? 1 : nspec;
+            int li = 1;
+            for (int p = 0; p < ns; ++p) {
+                const bool final_pass = p + 1 == ns;
+                CG_LAUNCH(KID_HIST, 0,
+                          k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], 0u, kc, wc, H, nbk, n,
+                                                                  B.rs, &B.rs->nactive, hsrc, bs, coord, segs, set_fs,
+                                                                  set_qb));
+                ++st->hist_passes;
+                CG_LAUNCH(KID_DECIDE, decide_bytes,
+                          k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[li], 0u, H, nbk, a.tolerance,
+                                                                         B.flags, B.rs, &B.rs->nactive, set_fs, set_qb,
+                                                                         B.list[li ^ 1], B.P[li ^ 1],
+                                                                         final_pass ? ch : no_ch));
+                li ^= 1;
+            }
+            active_list[L] = li;
+            // k_children returns at once if a segment is still searching
+            if (!fuse) {
+                const int rc_ = children();
+                if (rc_ != COUPE_ERR_OK) return rc_;
+            }
+        }
+        if (sync) {
             CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
             CG_CK(cudaStreamSynchronize(s));
-            if (h_rs->err) break;
-        }
-        if (h_rs->err) {
-            err_level = (int)L;
-            break;
-        }
-        if ((last && !fuse) || more) {
-            const int rc_ = children();
-            if (rc_ != COUPE_ERR_OK) return rc_;
-        }
-        if (!last && more) {
-            CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
-            CG_CK(cudaStreamSynchronize(s));
+            ++st->host_syncs;
             if (h_rs->err) {
                 err_level = (int)L;
-                break;
+                return -1;
+            }
+            // rare: splits that need more steps than the queued passes replay
+            int li = active_list[L], extra = 0;
+            bool more = false;
+            while (h_rs->nactive > 0) {
+                NvtxScope pass_range("rcb extra pass", (uint64_t)extra);
+                more = true;
+                if (++extra > 4096) {
+                    *err = "a split did not finish after 4096 passes";
+                    return COUPE_ERR_CRASH;
+                }
+                const uint64_t nlist = h_rs->nactive;
+                CG_LAUNCH(KID_HIST, h_rs->total_active * (sk + sw),
+                          k_hist<KT, WL><<<g_hist, BLOCK, 0, s>>>(segs, B.list[li], B.P[li], (uint32_t)nlist, kc, wc,
+                                                                  H, nbk, n, B.rs, nullptr, hsrc, bs, coord, segs,
+                                                                  set_fs, set_qb));
+                ++st->hist_passes;
+                CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
+                          k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
+                              segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, nullptr, set_fs,
+                              set_qb, B.list[li ^ 1], B.P[li ^ 1], no_ch));
+                li ^= 1;
+                CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+                CG_CK(cudaStreamSynchronize(s));
+                ++st->host_syncs;
+                if (h_rs->err) {
+                    err_level = (int)L;
+                    return -1;
+                }
+            }
+            if (more || resume) {
+                const int rc_ = children();
+                if (rc_ != COUPE_ERR_OK) return rc_;
             }
         }
         if (last) {
@@ -350,12 +411,12 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             if (multi) {
                 CG_LAUNCH(KID_ASSIGN, n * (D * sk + 8),
                           k_traverse_sets<D, KT><<<g_stream, BLOCK, 0, s>>>(B.trav, lv, B.keys[0][0], B.keys[0][1],
-                                                                            B.keys[0][2], n, ids, sets, bs));
+                                                                            B.keys[0][2], n, ids, sets, bs, B.rs));
                 bytes += n * (D * sk + 8);
             } else if (index_path) {
                 CG_LAUNCH(KID_ASSIGN, n * (sk + (ic ? 4 : 0) + 8),
-                          k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, (uint32_t)S, n, kc, ic, a.d_part, B.rs, bs,
-                                                                  coord));
+                          k_assign<KT><<<g_stream, BLOCK, 0, s>>>(segs, 0u, n, kc, ic, a.d_part, B.rs, bs, coord,
+                                                                  S_dev));
                 bytes += n * (sk + (ic ? 4 : 0) + 8);
             } else {
                 const uint64_t n_last = trav_used - lv.off[iters - 1];
@@ -385,9 +446,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                 bytes += n * (D * sk + 8);
             }
             st->levels = L + 1;
-            break;
+            return COUPE_ERR_OK;
         }
-        const uint64_t S_next = h_rs->nsegs_next, V_next = h_rs->items_next;
         const uint64_t chunk = chunk_of(V);
         const uint64_t nchunks = (V + chunk - 1) / chunk;
         if (nchunks > R0.lbcap) {
@@ -396,10 +456,10 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         }
         CG_CK(cudaMemsetAsync(B.lb, 0, nchunks * sizeof(uint64_t), s));
         CG_CK(cudaMemsetAsync(&B.rs->ticket, 0, sizeof(uint64_t), s));
-        const int kb_next = kb == 1 ? 2 : 1;
+        const int kb_next = key_buf(L + 1);
         ReorderArgs<D, KT, WL> R;
         R.segs = segs;
-        R.S = (uint32_t)S;
+        R.S = 0;
         R.n = V;
         R.chunk = chunk;
         R.nchunks = nchunks;
@@ -417,6 +477,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         R.lb = B.lb;
         R.rs = B.rs;
         R.spin_limit = (uint32_t)std::max(0, tu.lookback_spin_limit);
+        R.S_ptr = S_dev;
+        R.n_ptr = V_dev;
         const uint64_t rbytes = 2 * V * (D * sk + sw + si) - (ic ? 0 : V * si);
         const unsigned r_grid = (unsigned)std::min<uint64_t>(g_reorder, nchunks);
         if (carry) {
@@ -425,17 +487,59 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, false><<<r_grid, BLOCK, r_smem, s>>>(R));
         }
         bytes += V * sk /* flag pre-count */ + rbytes;
-        kb = kb_next;
-        sb = snext;
-        level0 = false;
-        S = S_next;
-        V = V_next;
-        nbk = pick_nbk(S_next);
         st->levels = L + 1;
+        return COUPE_ERR_OK;
+    };
+
+    // (the level counts of level 0, the root segments, are written by the
+    // root kernel)
+    auto finish = [&]() -> int {
+        CG_CK(cudaEventRecord(C.ev1, s));
+        CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
+        CG_CK(cudaStreamSynchronize(s));
+        ++st->host_syncs;
+        return COUPE_ERR_OK;
+    };
+    // Queue levels L.. to the end and wait once.  If a split of level L' needed
+    // a third pass, the queued kernels after it did nothing: finish L' with
+    // the host's further passes and queue L' + 1.. again.
+    uint64_t L = 0;
+    bool resume = false;
+    while (L < iters) {
+        if (resume || tu.sync_levels) {
+            const int rc_ = level(L, true, resume);
+            resume = false;
+            if (rc_ == -1) break;  // a device check failed (h_rs->err)
+            if (rc_ != COUPE_ERR_OK) return rc_;
+            ++L;
+            if (tu.sync_levels || L == iters) {
+                if (L == iters) {
+                    const int rf = finish();
+                    if (rf != COUPE_ERR_OK) return rf;
+                }
+                continue;
+            }
+        }
+        for (uint64_t l = L; l < iters; ++l) {
+            const int rc_ = level(l, false, false);
+            if (rc_ != COUPE_ERR_OK) return rc_;
+        }
+        const int rf = finish();
+        if (rf != COUPE_ERR_OK) return rf;
+        if (h_rs->err) {
+            err_level = (int)iters;  // seen after the queued levels
+            break;
+        }
+        if (!h_rs->stall) break;
+        L = h_rs->stall - 1;
+        resume = true;
+        nspec = std::min(nspec + 1, 3);  // the levels queued again get one more speculative pass
+        CG_CK(cudaMemsetAsync(&B.rs->stall, 0, sizeof(uint32_t), s));
     }
-    CG_CK(cudaEventRecord(C.ev1, s));
-    CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
-    CG_CK(cudaStreamSynchronize(s));
+    if (h_rs->err && tu.sync_levels) {
+        const int rf = finish();  // the stats below read h_rs after the last kernel
+        if (rf != COUPE_ERR_OK) return rf;
+    }
     C.prof.resolve();
     float ms = 0.f;
     cudaEventElapsedTime(&ms, C.ev0, C.ev1);
@@ -479,6 +583,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
 template <int D, class KT, class WT>
 int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err) {
     typedef typename KT::T K;
+    NvtxScope run_range(a.nsets > 1 ? "rcb batched run" : "rcb run");
     const Tuning &tu = tuning();
     const uint64_t n = a.n;
     cudaStream_t s = a.stream ? a.stream : C.stream;
@@ -520,14 +625,21 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     const uint64_t iters = max_iters;
     uint64_t scap = 1, tcap = 0;
     bool index_path = false;
+    std::vector<uint64_t> smax(iters), vmax(iters);
     if (multi) {
-        // level L holds at most min(2^L, n_k) segments of each set deeper than L
+        // level L holds at most min(2^L, n_k) segments of each set deeper
+        // than L, and every item of those sets
         for (uint64_t L = 0; L < iters && L < 64; ++L) {
-            uint64_t cnt = 0;
+            uint64_t cnt = 0, items = 0;
             for (uint32_t k : h_roots) {
                 const uint64_t nk = a.set_off[k + 1] - a.set_off[k];
-                if (a.set_iters[k] > L) cnt += L < 40 ? std::min<uint64_t>(nk, 1ull << L) : nk;
+                if (a.set_iters[k] > L) {
+                    cnt += L < 40 ? std::min<uint64_t>(nk, 1ull << L) : nk;
+                    items += nk;
+                }
             }
+            smax[L] = cnt;
+            vmax[L] = items;
             scap = std::max(scap, cnt);
             tcap += cnt;
         }
@@ -547,6 +659,10 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
         for (uint64_t L = 0; L < iters && tcap <= TRAV_MAX_ENTRIES; ++L)
             tcap += L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
         index_path = tu.force_index_path || iters > (uint64_t)MAX_TRAV_LEVELS || tcap > TRAV_MAX_ENTRIES;
+        for (uint64_t L = 0; L < iters; ++L) {
+            smax[L] = L < 40 ? std::min<uint64_t>(n, 1ull << L) : n;
+            vmax[L] = n;
+        }
     }
     const uint64_t hb = std::max<uint64_t>(2 * scap, std::min<uint64_t>(scap * MAX_NB, 1ull << 22));
     // look-back words: one per reorder chunk; a reorder grid never exceeds 8
@@ -557,13 +673,13 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     Bump dry{nullptr, 0};
     const bool carry = index_path || KT::BAND;
     const uint64_t nsets = multi ? a.nsets : 0;
-    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
+    const size_t need = B.carve(dry, n, scap, hb, lbcap, index_path, carry, tcap, nsets, iters);
     // 256 bytes of slack: reorder tiles are copied in 16-byte chunks that may
     // end up to 15 bytes past a buffer
     int rc = ensure_workspace(C, need + 256, err);
     if (rc != COUPE_ERR_OK) return rc;
     Bump real{(char *)C.ws, 0};
-    B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap, nsets);
+    B.carve(real, n, scap, hb, lbcap, index_path, carry, tcap, nsets, iters);
     const SetTab sets = B.set_tab(multi ? (uint32_t)a.nsets : 1u);
     RunScalars *h_rs = (RunScalars *)C.h_pinned;
 
@@ -624,12 +740,15 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     R0.h_rs = h_rs;
     R0.g_stream = g_stream;
     R0.lbcap = lbcap;
+    R0.smax = std::move(smax);
+    R0.vmax = std::move(vmax);
     // algorithmic bytes: the input read and the SoA keys written
     R0.bytes = n * (D * 8 + sw) + n * D * sk + n * sw + (c16 ? n * 2 : 0);  // convert + weight sum
     if (WT::LIMBS > 1) R0.bytes += n * sw;
     if constexpr (WT::LIMBS == 1) {
         CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
         CG_CK(cudaStreamSynchronize(s));
+        ++st->host_syncs;
         if (h_rs->narrow16 == 0) return run_levels<D, KT, WT, WtC16<WT>>(C, a, st, err, B, R0, c16);
     }
     return run_levels<D, KT, WT, WT>(C, a, st, err, B, R0, w_in);

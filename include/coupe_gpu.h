@@ -52,6 +52,7 @@ struct coupe_gpu_stats {
 	 * quantum each) and the exact fixed-point total is rounded once to f64;
 	 * 0 for integer weights (exact, wrapping sums). */
 	double weight_sum_error_bound;
+	uint64_t host_syncs;      /* host synchronisations of the level loop */
 };
 
 /* coupe_rcb with an explicit precision mode. */
@@ -261,6 +262,11 @@ const char *coupe_gpu_kernel_name(int id);
  *                             every pass (by default the bins hold truncated
  *                             sums and a decision they cannot settle is
  *                             replayed from exact bins)
+ *   "sync_levels"             1: the host waits for each tree level before
+ *                             queuing the next (by default a run is queued
+ *                             whole and waited for once; a split needing more
+ *                             than two histogram passes makes the host finish
+ *                             from that level on level by level)
  * and two failure-handling knobs:
  *   "lookback_spin_limit"     polls of a reorder chunk's wait for its
  *                             predecessor's prefix before the run fails with

@@ -289,7 +289,8 @@ def test_rib_end_to_end(coupe, oracle_mod):
                                    {"reorder_chunks_per_cta": 4}, {"reorder_chunks_per_cta": 64},
                                    {"max_nbk": 5, "reorder_chunks_per_cta": 3},
                                    {"force_index_path": 1, "reorder_chunks_per_cta": 7},
-                                   {"hist_ctas_per_sm": 1}, {"hist_ctas_per_sm": 2, "max_nbk": 9}])
+                                   {"hist_ctas_per_sm": 1}, {"hist_ctas_per_sm": 2, "max_nbk": 9},
+                                   {"sync_levels": 1}, {"sync_levels": 1, "max_nbk": 2}, {"max_nbk": 2}])
 def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     """Part ids through the index path, fewer bisection steps per pass and
     other chunkings equal the oracle's."""
@@ -499,3 +500,29 @@ def test_pinned_host_buffers(coupe, oracle_mod):
             finally:
                 for k, v in old.items():
                     coupe.set_option(k, v)
+
+
+@pytest.mark.parametrize("mode", ["ref32", "f32key_f64band"])
+def test_queued_run_waits_once(coupe, oracle_mod, mode):
+    """A run is queued whole: the host waits for the 16-bit weight check and
+    for the end (2 synchronisations), against one per level with
+    sync_levels; a split needing more than two histogram passes (max_nbk 2)
+    halts the queue and the host finishes level by level.  Same ids."""
+    from coupe_gb300 import workloads
+    pts, w, _ = workloads.gaussian_mixture3d(n=200_000, seed=12)
+    om = oracle_mod.REF32 if mode == "ref32" else oracle_mod.F64
+    want, _ = oracle_mod.rcb(pts, w, 9, 0.01, mode=om)
+    assert (_gpu(coupe, pts, w, 9, 0.01, mode=mode) == want).all()
+    assert coupe.last_stats()["host_syncs"] <= 2
+    old = {k: coupe.get_option(k) for k in ("sync_levels", "max_nbk")}
+    try:
+        coupe.set_option("sync_levels", 1)
+        assert (_gpu(coupe, pts, w, 9, 0.01, mode=mode) == want).all()
+        assert coupe.last_stats()["host_syncs"] >= 9
+        coupe.set_option("sync_levels", 0)
+        coupe.set_option("max_nbk", 2)
+        assert (_gpu(coupe, pts, w, 9, 0.01, mode=mode) == want).all()
+        assert coupe.last_stats()["host_syncs"] > 2  # halted, then level by level
+    finally:
+        for k, v in old.items():
+            coupe.set_option(k, v)
