@@ -20,6 +20,7 @@ import numpy as np
 __all__ = [
     "Rcb", "Rib", "CoupeError", "lib", "library_path", "MODES", "last_stats",
     "rcb_device", "rib_device", "rib_matrix_device", "rcb_batched_device", "autotune_device",
+    "MultiJagged", "multi_jagged_device", "axis_sort_device",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -43,6 +44,7 @@ EXPORTED = [
     "coupe_gpu_split_noalloc", "coupe_gpu_rcb_batched", "coupe_gpu_autotune",
     "coupe_gpu_parts_load", "coupe_gpu_imbalance", "coupe_gpu_parts_load_device", "coupe_gpu_imbalance_device",
     "coupe_gpu_barycentres", "coupe_gpu_grid_rcb", "coupe_gpu_grid_rcb_device",
+    "coupe_gpu_axis_sort_device", "coupe_gpu_multi_jagged", "coupe_gpu_multi_jagged_device",
 ]
 
 
@@ -144,6 +146,12 @@ def lib():
     L.coupe_gpu_grid_rcb_device.argtypes = [vp, u64, vp, i32, vp, u64, u64, vp]
     L.coupe_gpu_grid_rcb_device.restype = i32
     L.coupe_gpu_barycentres.argtypes = [u64, u64, vp, u64, u64, vp, vp, vp]
+    L.coupe_gpu_axis_sort_device.argtypes = [vp, u64, u64, vp, u64, vp]
+    L.coupe_gpu_axis_sort_device.restype = i32
+    L.coupe_gpu_multi_jagged.argtypes = [vp, u64, vp, vp, u64, u64]
+    L.coupe_gpu_multi_jagged.restype = i32
+    L.coupe_gpu_multi_jagged_device.argtypes = [vp, u64, u64, vp, vp, u64, u64, vp]
+    L.coupe_gpu_multi_jagged_device.restype = i32
     L.coupe_gpu_barycentres.restype = i32
     L.coupe_gpu_set_option.argtypes = [ctypes.c_char_p, ctypes.c_int64]
     L.coupe_gpu_set_option.restype = i32
@@ -541,4 +549,55 @@ def rib_matrix_device(points, stream=None, weights=None):
         wt = {torch.int32: COUPE_INT, torch.int64: COUPE_INT64, torch.float64: COUPE_DOUBLE}[weights.dtype]
         _check(lib().coupe_gpu_rib_matrix_weighted(n, dim, _ptr(points), wt, _ptr(weights), out.ctypes.data,
                                                    ctypes.c_void_p(s)))
+    return out
+
+
+@dataclass
+class MultiJagged:
+    """coupe::MultiJagged (coupe/src/algorithms/multi_jagged.rs:368-385):
+    part_count parts in at most max_iter iterations.  partition(part_ids,
+    (points, weights)) with float64 points (N, D) and float64 weights."""
+    part_count: int
+    max_iter: int
+
+    def partition(self, part_ids, data):
+        points, weights = data
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        if pts.ndim != 2:
+            raise ValueError("points must be (N, D)")
+        w = (np.full(len(pts), weights, dtype=np.float64) if np.isscalar(weights)
+             else np.ascontiguousarray(weights, dtype=np.float64))
+        if part_ids.dtype not in (np.uint64, np.int64) or not part_ids.flags.c_contiguous:
+            raise TypeError("part_ids must be a contiguous uint64/int64 array")
+        L = lib()
+        dp = L.coupe_data_array(len(pts), COUPE_DOUBLE, pts.ctypes.data)
+        dw = L.coupe_data_array(len(w), COUPE_DOUBLE, w.ctypes.data)
+        try:
+            rc = L.coupe_gpu_multi_jagged(part_ids.ctypes.data, pts.shape[1], dp, dw, self.part_count,
+                                          self.max_iter)
+        finally:
+            L.coupe_data_free(dp)
+            L.coupe_data_free(dw)
+        _check(rc)
+
+
+def multi_jagged_device(part_ids, points, weights, part_count, max_iter, stream=None):
+    """MultiJagged on CUDA tensors: part_ids int64/uint64 (N,), points
+    float64 (N, D), weights float64 (N,)."""
+    import torch
+    n, dim = points.shape
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    rc = lib().coupe_gpu_multi_jagged_device(_ptr(part_ids), n, dim, _ptr(points), _ptr(weights), part_count,
+                                             max_iter, ctypes.c_void_p(s))
+    _check(rc)
+
+
+def axis_sort_device(points, coord, stream=None):
+    """coupe's axis_sort of 0..N-1 along `coord` on CUDA float64 points
+    (N, D); returns an int64 tensor of point indices (ties in index order)."""
+    import torch
+    n, dim = points.shape
+    out = torch.empty(n, dtype=torch.int64, device=points.device)
+    s = stream.cuda_stream if stream is not None else torch.cuda.current_stream().cuda_stream
+    _check(lib().coupe_gpu_axis_sort_device(_ptr(out), n, dim, _ptr(points), coord, ctypes.c_void_p(s)))
     return out

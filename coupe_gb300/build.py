@@ -29,7 +29,7 @@ NVFLAGS = ARCH + [
 ]
 
 SOURCES = ["engine_core.cu", "inst_ref32.cu", "inst_f64.cu", "inst_band.cu", "split_noalloc.cu", "imbalance.cu",
-           "mesh.cu", "grid.cu", "ffi.cpp"]
+           "mesh.cu", "grid.cu", "multi_jagged.cu", "ffi.cpp"]
 
 
 def _deps_mtime():

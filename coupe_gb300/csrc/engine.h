@@ -60,6 +60,9 @@ struct Tuning {
     // once, finishing level by level only after a split needed a third pass.
     // The ids are the same.
     int sync_levels = 0;
+    // 1: coupe_gpu_autotune returns the schedule kept for a workload class
+    // tuned before (in this process, or in the COUPE_GPU_TUNE_CACHE file)
+    int autotune_cache = 1;
 };
 Tuning &tuning();
 
@@ -148,6 +151,17 @@ int barycentres(DevCtx &C, int dim, const double *d_coords, uint64_t n_nodes, ui
 
 // The engine's per-point f64 -> f32 key conversion over n device values.
 int f64_to_f32(DevCtx &C, const double *d_in, float *d_out, uint64_t n, cudaStream_t stream, std::string *err);
+
+// coupe's axis_sort of the identity permutation of n device points of `dim`
+// doubles along `coord` (recursive_bisection.rs:815-827): d_perm gets the
+// point indices in ascending coordinate order, ties in index order.
+int axis_sort(DevCtx &C, uint64_t n, int dim, const double *d_points, int coord, uint64_t *d_perm,
+              cudaStream_t stream, std::string *err);
+
+// coupe's MultiJagged (multi_jagged.rs:150-295) of n device points with f64
+// weights into part_count parts in at most max_iter iterations.
+int multi_jagged(DevCtx &C, uint64_t n, int dim, const double *d_points, const double *d_weights,
+                 uint64_t part_count, uint64_t max_iter, uint64_t *d_part, cudaStream_t stream, std::string *err);
 
 // Per-mode entry points, instantiated in separate translation units.
 int run_rcb_ref32(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err);

@@ -8,9 +8,12 @@
 // memory, copied to the device, partitioned there, and the ids copied back.
 #include <cuda_runtime.h>
 
+#include <cstdio>
 #include <cstdlib>
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -716,6 +719,118 @@ enum coupe_err coupe_gpu_grid_rcb(uintptr_t *partition, uintptr_t dimension, con
     return COUPE_ERR_OK;
 }
 
+enum coupe_err coupe_gpu_axis_sort_device(uint64_t *d_permutation, uint64_t n, uint64_t dimension,
+                                         const double *d_points, uint64_t coord, void *stream) {
+    t_err.clear();
+    if (dimension == 0 || dimension > 64 || coord >= dimension) return COUPE_ERR_BAD_DIMENSION;
+    if (n == 0) return COUPE_ERR_OK;
+    if (!d_permutation || !d_points) {
+        t_err = "NULL permutation or points";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    const int rc = cg::axis_sort(*C, n, (int)dimension, d_points, (int)coord, d_permutation, (cudaStream_t)stream,
+                                 &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+enum coupe_err coupe_gpu_multi_jagged_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
+                                             const double *d_points, const double *d_weights, uint64_t part_count,
+                                             uint64_t max_iter, void *stream) {
+    t_err.clear();
+    if (dimension == 0 || dimension > 64) return COUPE_ERR_BAD_DIMENSION;
+    if (n == 0) return COUPE_ERR_OK;
+    if (!d_partition || !d_points || !d_weights) {
+        t_err = "NULL partition, points or weights";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    std::lock_guard<std::mutex> lock(C->mu);
+    const int rc = cg::multi_jagged(*C, n, (int)dimension, d_points, d_weights, part_count, max_iter, d_partition,
+                                    (cudaStream_t)stream, &err);
+    if (rc != COUPE_ERR_OK) t_err = err;
+    return (coupe_err)rc;
+}
+
+enum coupe_err coupe_gpu_multi_jagged(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+                                      const coupe_data *weights, uintptr_t part_count, uintptr_t max_iter) {
+    t_err.clear();
+    if (!points || !weights) {
+        t_err = "NULL data set";
+        return COUPE_ERR_CRASH;
+    }
+    const uintptr_t n = points->len;
+    if (n != weights->len) return COUPE_ERR_LEN_MISMATCH;
+    if (dimension == 0 || dimension > 64) return COUPE_ERR_BAD_DIMENSION;
+    if (weights->type != COUPE_DOUBLE) {
+        t_err = "MultiJagged takes double weights";
+        return COUPE_ERR_BAD_TYPE;
+    }
+    if (n == 0) return COUPE_ERR_OK;
+    if (!partition) {
+        t_err = "NULL partition";
+        return COUPE_ERR_CRASH;
+    }
+    std::string err;
+    cg::DevCtx *C = cg::device_ctx(&err);
+    if (!C) {
+        t_err = err;
+        return COUPE_ERR_CRASH;
+    }
+    const size_t pbytes = (size_t)n * dimension * sizeof(double), wbytes = (size_t)n * 8, obytes = (size_t)n * 8;
+    std::lock_guard<std::mutex> lock(C->mu);
+    char *dbuf = (char *)t_dev.get(pbytes + wbytes + obytes + 512, C->dev);
+    if (!dbuf) {
+        t_err = "device allocation of the input copy failed";
+        return COUPE_ERR_ALLOC;
+    }
+    double *d_pts = (double *)dbuf;
+    double *d_w = (double *)(dbuf + ((pbytes + 255) & ~(size_t)255));
+    uint64_t *d_part = (uint64_t *)((char *)d_w + ((wbytes + 255) & ~(size_t)255));
+    static thread_local Staging st_p, st_w;
+    const void *src_p = points->ptr;
+    if (points->kind != 0) {
+        double *h = (double *)st_p.get(pbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(points, i, dimension * sizeof(double), h + i * dimension);
+        src_p = h;
+    }
+    const void *src_w = weights->ptr;
+    if (weights->kind != 0) {
+        char *h = (char *)st_w.get(wbytes);
+        if (!h) return COUPE_ERR_ALLOC;
+        for (uintptr_t i = 0; i < n; ++i) fetch(weights, i, 8, h + i * 8);
+        src_w = h;
+    }
+    cudaStream_t s = C->stream;
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(d_pts, src_p, pbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(d_w, src_w, wbytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "host to device copy", &t_err);
+    const int rc = cg::multi_jagged(*C, n, (int)dimension, d_pts, d_w, part_count, max_iter, d_part, s, &err);
+    if (rc != COUPE_ERR_OK) {
+        cudaStreamSynchronize(s);
+        t_err = err;
+        return (coupe_err)rc;
+    }
+    if ((e = cudaMemcpyAsync(partition, d_part, obytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return (coupe_err)cg::cuda_fail(e, "device to host copy", &t_err);
+    return COUPE_ERR_OK;
+}
+
 enum coupe_err coupe_gpu_barycentres(uint64_t dimension, uint64_t n_nodes, const double *d_coords,
                                      uint64_t n_elements, uint64_t nodes_per_element, const uint64_t *d_nodes,
                                      double *d_out, void *stream) {
@@ -813,6 +928,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "lookback_spin_limit")) return &t.lookback_spin_limit;
     if (!std::strcmp(name, "workspace_limit_mb")) return &t.workspace_limit_mb;
     if (!std::strcmp(name, "sync_levels")) return &t.sync_levels;
+    if (!std::strcmp(name, "autotune_cache")) return &t.autotune_cache;
     return nullptr;
 }
 
@@ -828,6 +944,68 @@ int64_t coupe_gpu_get_option(const char *name) {
     return p ? *p : -1;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The autotuner's choices by workload class: the number of points and of sets
+// (powers of two), the dimension, weight type, precision mode and deepest
+// iteration count.  Kept for the process and, when the environment variable
+// COUPE_GPU_TUNE_CACHE names a file, in that file (one line per class,
+// appended when a class is first tuned, read at the first lookup).
+struct TuneEntry {
+    int max_nbk, hist_ctas_per_sm, reorder_chunks_per_cta;
+    double ms;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneEntry> g_tune;
+bool g_tune_loaded = false;
+
+int log2_floor(uint64_t v) {
+    int l = 0;
+    while (v > 1) {
+        v >>= 1;
+        ++l;
+    }
+    return l;
+}
+
+std::string tune_key(uint64_t n, uint64_t nsets, uint64_t dim, int wtype, int mode, uint32_t iters) {
+    char b[96];
+    snprintf(b, sizeof(b), "n2^%d/sets2^%d/d%llu/w%d/m%d/it%u", log2_floor(n), log2_floor(nsets),
+             (unsigned long long)dim, wtype, mode, iters);
+    return b;
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = std::getenv("COUPE_GPU_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE *f = std::fopen(path, "r");
+    if (!f) return;
+    char key[128];
+    TuneEntry e;
+    while (std::fscanf(f, "%127s %d %d %d %lf", key, &e.max_nbk, &e.hist_ctas_per_sm, &e.reorder_chunks_per_cta,
+                       &e.ms) == 5)
+        g_tune[key] = e;
+    std::fclose(f);
+}
+
+void tune_store_locked(const std::string &key, const TuneEntry &e) {
+    g_tune[key] = e;
+    const char *path = std::getenv("COUPE_GPU_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE *f = std::fopen(path, "a");
+    if (!f) return;
+    std::fprintf(f, "%s %d %d %d %.6f\n", key.c_str(), e.max_nbk, e.hist_ctas_per_sm, e.reorder_chunks_per_cta, e.ms);
+    std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" {
+
 enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const uint64_t *set_offsets,
                                   uint64_t dimension, const double *d_points, enum coupe_type weight_type,
                                   const void *d_weights, const uint32_t *iter_counts, double tolerance, int mode,
@@ -838,6 +1016,28 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
     cg::Tuning &t = cg::tuning();
     const cg::Tuning keep = t;
     const int reps = repeats < 1 ? 1 : (repeats > 15 ? 15 : repeats);
+    // a workload class tuned before: its schedule, without timing
+    uint32_t it_max = 0;
+    for (uint64_t k = 0; k < nsets && iter_counts; ++k) it_max = std::max(it_max, iter_counts[k]);
+    const uint64_t npts = nsets && set_offsets ? set_offsets[nsets] : 0;
+    const std::string key = tune_key(npts, nsets, dimension, (int)weight_type, mode, it_max);
+    if (cg::tuning().autotune_cache) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_load_locked();
+        auto hit = g_tune.find(key);
+        if (hit != g_tune.end()) {
+            t.max_nbk = hit->second.max_nbk;
+            t.hist_ctas_per_sm = hit->second.hist_ctas_per_sm;
+            t.reorder_chunks_per_cta = hit->second.reorder_chunks_per_cta;
+            if (best) {
+                best->max_nbk = t.max_nbk;
+                best->hist_ctas_per_sm = t.hist_ctas_per_sm;
+                best->reorder_chunks_per_cta = t.reorder_chunks_per_cta;
+                best->device_ms = hit->second.ms;
+            }
+            return COUPE_ERR_OK;
+        }
+    }
     double best_ms = 1e300;
     cg::Tuning best_t = keep;
     for (int nbk : {10, 9, 8, 7, 6})
@@ -866,6 +1066,11 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
                 }
             }
     t = best_t;
+    if (cg::tuning().autotune_cache) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_store_locked(key, TuneEntry{best_t.max_nbk, best_t.hist_ctas_per_sm, best_t.reorder_chunks_per_cta,
+                                         best_ms});
+    }
     if (best) {
         best->max_nbk = best_t.max_nbk;
         best->hist_ctas_per_sm = best_t.hist_ctas_per_sm;

@@ -29,8 +29,8 @@ enum coupe_err {
 	COUPE_ERR_BAD_TYPE,      /* unsupported element type or value */
 	COUPE_ERR_BIPART_ONLY,   /* kept for ABI compatibility; never returned here */
 	COUPE_ERR_LEN_MISMATCH,  /* points and weights differ in length */
-	COUPE_ERR_NOT_FOUND,     /* kept for ABI compatibility; never returned by rcb/rib */
-	COUPE_ERR_NEG_VALUES,    /* kept for ABI compatibility; never returned here */
+	COUPE_ERR_NOT_FOUND,     /* never returned by rcb/rib; multi_jagged: no partition scheme */
+	COUPE_ERR_NEG_VALUES,    /* never returned by rcb/rib; multi_jagged: a negative weight */
 };
 
 /* Static, NUL-terminated message for an error code.

@@ -163,6 +163,37 @@ enum coupe_err coupe_gpu_grid_rcb_device(uint64_t *d_partition, uint64_t dimensi
 		enum coupe_type weight_type, const void *d_weights, uint64_t iter_count, uint64_t threads,
 		void *stream);
 
+/* coupe's axis_sort (coupe/src/algorithms/recursive_bisection.rs:815-827,
+ * the sort MultiJagged applies per iteration): d_permutation gets 0..n-1
+ * ordered by coordinate `coord` of the n device points (n x dimension
+ * doubles).  coupe's sort is unstable; this one keeps equal coordinates in
+ * index order (-0.0 sorts before +0.0), so results equal coupe's wherever
+ * the coordinates are distinct.  dimension 1..64 and coord < dimension, else
+ * COUPE_ERR_BAD_DIMENSION.  Returns after the work on `stream` completed. */
+enum coupe_err coupe_gpu_axis_sort_device(uint64_t *d_permutation, uint64_t n, uint64_t dimension,
+		const double *d_points, uint64_t coord, void *stream);
+
+/* MultiJagged (coupe::MultiJagged, coupe/src/algorithms/multi_jagged.rs:
+ * 150-295, 368-385; coupe-ffi has no binding for it): part_count parts in at
+ * most max_iter iterations following coupe's partition scheme; iteration k
+ * sorts every part along axis k % dimension and cuts it at the running
+ * weights total * modifier, a cut moving past every point whose running
+ * weight is within 4 ulps of the threshold.  Part ids are numbered as coupe
+ * numbers them with one rayon worker (depth first).  Running weights are the
+ * exact sums of the sorted weights rounded once (coupe's are sequential f64
+ * sums of rayon chunks), so a cut can differ from coupe's only where these
+ * differ in the last bits.  Weights: double, finite and non-negative
+ * (COUPE_ERR_BAD_TYPE, COUPE_ERR_NEG_VALUES; coupe does not check).
+ * Errors: COUPE_ERR_LEN_MISMATCH, COUPE_ERR_BAD_DIMENSION (dimension 1..64),
+ * COUPE_ERR_BAD_TYPE for part_count 0, COUPE_ERR_NOT_FOUND when no scheme of
+ * part_count parts in max_iter iterations exists (coupe panics),
+ * COUPE_ERR_ALLOC for n >= 2^32 or part_count > 2^24. */
+enum coupe_err coupe_gpu_multi_jagged(uintptr_t *partition, uintptr_t dimension, const coupe_data *points,
+		const coupe_data *weights, uintptr_t part_count, uintptr_t max_iter);
+enum coupe_err coupe_gpu_multi_jagged_device(uint64_t *d_partition, uint64_t n, uint64_t dimension,
+		const double *d_points, const double *d_weights, uint64_t part_count, uint64_t max_iter,
+		void *stream);
+
 /* Barycentres of one block of mesh elements with the same node count
  * (mesh-part's points, tools/lib/lib.rs:511-539): element e's point is the
  * sum of the coordinates of its nodes d_nodes[e * nodes_per_element + j]
@@ -262,6 +293,9 @@ const char *coupe_gpu_kernel_name(int id);
  *                             every pass (by default the bins hold truncated
  *                             sums and a decision they cannot settle is
  *                             replayed from exact bins)
+ *   "autotune_cache"          1 (default): coupe_gpu_autotune returns the
+ *                             schedule kept for a workload class tuned before
+ *                             without timing again; 0: always time
  *   "sync_levels"             1: the host waits for each tree level before
  *                             queuing the next (by default a run is queued
  *                             whole and waited for once; a split needing more
@@ -296,7 +330,13 @@ struct coupe_gpu_tuning {
  * every schedule).  `best` (may be NULL) receives the choice; d_partition
  * holds the ids of the last run.  30 candidates (bisection steps per pass
  * 6-10, histogram CTAs per SM 0/3/2, reorder chunks per CTA 1/2): budget
- * about 30 * (repeats + 1) runs of the workload. */
+ * about 30 * (repeats + 1) runs of the workload.  The choice is kept per
+ * workload class (points and sets rounded down to powers of two, dimension,
+ * weight type, mode, deepest iteration count): a later call for the same
+ * class applies the kept schedule at once, runs nothing and leaves
+ * d_partition untouched (option autotune_cache).  When the environment
+ * variable COUPE_GPU_TUNE_CACHE names a file, the choices are also read from
+ * it and appended to it, so that they outlive the process. */
 enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets,
 		const uint64_t *set_offsets, uint64_t dimension, const double *d_points,
 		enum coupe_type weight_type, const void *d_weights,

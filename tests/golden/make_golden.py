@@ -7,7 +7,7 @@ prints its partitions without asserting them; its expected ids are derived by
 hand from recursive_bisection.rs:456-705 (iter_count 1 splits x at 0.5;
 iter_count 2 then splits y at 0.5 in both halves).
 
-Usage: python tests/golden/make_golden.py [/path/to/coupe]
+Usage: python tests/golden/make_golden.py /path/to/coupe
 """
 import json
 import os
@@ -83,10 +83,26 @@ def main(root):
         "source": rb + ":952-983",
         "inputs": "1..23 positive f32 keys, every index as the pivot",
         "expect": "left < pivot <= right; each key on exactly one side"}
+    mj = "coupe/src/algorithms/multi_jagged.rs"
+    sample = points(lines(root, rb, 940, 950))
+    cases["axis_sort_x"] = {
+        "source": rb + ":1021-1029", "points": sample, "coord": 0,
+        "expect": [int(x) for x in re.findall(r"\d+", lines(root, rb, 1028, 1028).split("vec!")[1])]}
+    cases["axis_sort_y"] = {
+        "source": rb + ":1031-1039", "points": sample, "coord": 1,
+        "expect": [int(x) for x in re.findall(r"\d+", lines(root, rb, 1038, 1038).split("vec!")[1])]}
+    cases["multi_jagged_doctest"] = {
+        "source": mj + ":333-365", "points": points(lines(root, mj, 338, 348)),
+        "weights": "f64 4.2 each", "part_count": 9, "max_iter": 4, "expect": "all ids distinct"}
+    cases["split_at_mut_many"] = {
+        "source": mj + ":416-433", "len": 13, "positions": [1, 3, 6, 9, 11],
+        "expect": [[0], [1, 2], [3, 4, 5], [6, 7, 8], [9, 10], [11, 12]]}
     with open(os.path.join(HERE, "reference_known_answers.json"), "w") as f:
         json.dump(cases, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_known_answers.json"))
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py /path/to/coupe (the reference's source tree)")
+    main(sys.argv[1])

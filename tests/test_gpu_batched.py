@@ -141,8 +141,9 @@ def test_autotune_keeps_ids(coupe, oracle_mod):
     pts, w, off, it = _sets(rng, sizes, 3, "i64", iters)
     want = oracle_mod.rcb_sets(pts, w, off, it, 0.01, mode=1, threads=0)
     names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta")
-    keep = {k: coupe.get_option(k) for k in names}
+    keep = {k: coupe.get_option(k) for k in names + ("autotune_cache",)}
     try:
+        coupe.set_option("autotune_cache", 0)  # time the candidates here
         dp = torch.from_numpy(pts).cuda()
         dw = torch.from_numpy(w).cuda()
         ids = torch.zeros(len(pts), dtype=torch.int64, device="cuda")
@@ -152,6 +153,39 @@ def test_autotune_keeps_ids(coupe, oracle_mod):
         assert {k: coupe.get_option(k) for k in names} == {k: best[k] for k in names}
         assert np.array_equal(ids.cpu().numpy().astype(np.uint64), want)
         assert np.array_equal(_gpu(coupe, torch, pts, w, off, it, 0.01, "f32key_f64band"), want)
+    finally:
+        for k, v in keep.items():
+            coupe.set_option(k, v)
+
+
+def test_autotune_keeps_its_choice_per_workload_class(coupe, tmp_path, monkeypatch):
+    """A second call for the same workload class applies the kept schedule
+    without running; the choice is written to COUPE_GPU_TUNE_CACHE."""
+    torch = pytest.importorskip("torch")
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("COUPE_GPU_TUNE_CACHE", str(cache))
+    rng = np.random.default_rng(22)
+    sizes = [int(x) for x in rng.integers(5_000, 50_000, 9)]
+    iters = np.full(len(sizes), 7)
+    pts, w, off, it = _sets(rng, sizes, 2, "i32", iters)
+    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta")
+    keep = {k: coupe.get_option(k) for k in names + ("autotune_cache",)}
+    try:
+        coupe.set_option("autotune_cache", 1)
+        dp = torch.from_numpy(pts).cuda()
+        dw = torch.from_numpy(w).cuda()
+        ids = torch.zeros(len(pts), dtype=torch.int64, device="cuda")
+        first = coupe.autotune_device(ids, dp, dw, off, it, 0.02, mode="ref32", repeats=1)
+        for k, v in keep.items():  # another schedule in force
+            coupe.set_option(k, v)
+        coupe.set_option("autotune_cache", 1)
+        ids2 = torch.full((len(pts),), 7, dtype=torch.int64, device="cuda")
+        again = coupe.autotune_device(ids2, dp, dw, off, it, 0.02, mode="ref32", repeats=1)
+        assert again == first
+        assert {k: coupe.get_option(k) for k in names} == {k: first[k] for k in names}
+        assert (ids2 == 7).all()  # nothing ran
+        lines = cache.read_text().split("\n")
+        assert any(l.startswith("n2^") and l.split()[1] == str(first["max_nbk"]) for l in lines)
     finally:
         for k, v in keep.items():
             coupe.set_option(k, v)
