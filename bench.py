@@ -6,7 +6,7 @@ Inputs are 537 MB per step (larger than the 129 MB L2), so no L2 flush is
 needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload gauss16M|planes67M|batched4096|hexrib134M]
+                  [--workload gauss16M|uniform1M|planes67M|batched4096|hexrib134M]
 
 `value`   device-resident throughput (inputs in HBM before the timed region),
           Mpoints/s, of the headline precision mode.
@@ -19,9 +19,12 @@ needed between steps.
 --impl reference times that CPU restatement alone (the reference itself is
 Rust and cannot be built here).
 
-The other workloads (--workload) print one line of the same form for the
-precision form on 67M points (4096 parts, f64 weights), the batched form
-(4096 sets, ~2e8 points) and Rib on a 512^3 hex mesh (134M points).
+The other workloads (--workload) print one line of the same form for plain
+Rcb of 1M 2D points (8 parts, unit weights; inputs below L2 size, so L2 is
+flushed before each timed step), the precision form on 67M points (4096
+parts, f64 weights), the batched form (4096 sets, ~2e8 points) and Rib on a
+512^3 hex mesh (134M points); with --impl reference, the CPU restatement's
+line for the same workload.
 """
 import argparse
 import json
@@ -39,6 +42,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "RCB Mpoints/s, 16M 3D pts→1024 parts: FP32-key+FP64-band vs plain FP64 on GB300"
 UNIT = "Mpoints/s"
+L2_FLUSH_BELOW = 256 << 20  # inputs below this size: L2 is flushed before each timed step
 
 
 def parse():
@@ -49,7 +53,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--points", type=int, default=16_777_216)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", default="gauss16M", choices=["gauss16M", "planes67M", "batched4096", "hexrib134M"])
+    ap.add_argument("--workload", default="gauss16M", choices=["gauss16M", "uniform1M", "planes67M", "batched4096", "hexrib134M"])
     return ap.parse_args()
 
 
@@ -194,10 +198,10 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.impl == "reference":
+        return run_reference(args) if args.workload == "gauss16M" else run_reference_workload(args)
     if args.workload != "gauss16M":
         return run_workload(args)
-    if args.impl == "reference":
-        return run_reference(args)
     import torch
     import torch.distributed as dist
     import coupe_gb300 as coupe
@@ -271,7 +275,7 @@ def main():
     top = max(prof.items(), key=lambda kv: kv[1]["ms"])
     peak, peak_kind = measured_peak()
     achieved = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9
-    traffic = _traffic_per_launch(top[0], headline)
+    traffic = _traffic_per_launch(top[0], headline, "gauss16M")
     roofline = {"bound": "hbm", "kernel": top[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "traffic": traffic, "algorithmic_bytes_per_launch": top[1]["bytes"] // max(1, top[1]["launches"]),
@@ -419,13 +423,115 @@ def main():
     return 0
 
 
+def _load_workload(name):
+    """Host arrays and the printed description of a non-headline workload
+    (both arms print the same `metric` and `config`)."""
+    from coupe_gb300 import workloads
+    if name == "batched4096":
+        groups = workloads.batched_groups()
+        n = sum(len(g[0]) for g in groups.values())
+        cfg = {"workload": "batched_4096sets", "sets": 4096, "points": n, "dim": "2 and 3 (one call each)",
+               "iter_count": "U{1..8} per set", "tolerance": 0.01, "weights": "int64 U{1..10}", "algorithm": "Rcb",
+               "l2": _l2_note(sum(g[0].nbytes + g[1].nbytes for g in groups.values()))}
+        return {"batched": True, "groups": groups, "n": n, "tol": 0.01, "cfg": cfg, "rib": False, "float": False}
+    if name == "uniform1M":
+        pts, w, c = workloads.uniform2d_unit()
+        weights = "int64 1"
+    elif name == "hexrib134M":
+        pts, w, c = workloads.hex_mesh_rib()
+        weights = "float64"
+    else:
+        pts, w, c = workloads.planes3d_lognormal()
+        weights = "float64"
+    rib = name == "hexrib134M"
+    cfg = {"workload": c["name"], "points": len(pts), "dim": pts.shape[1], "parts": 1 << c["iter_count"],
+           "iter_count": c["iter_count"], "tolerance": c["tolerance"], "weights": weights,
+           "algorithm": "Rib" if rib else "Rcb", "l2": _l2_note(pts.nbytes + w.nbytes)}
+    return {"batched": False, "pts": pts, "w": w, "n": len(pts), "iters": c["iter_count"], "tol": c["tolerance"],
+            "cfg": cfg, "rib": rib, "float": w.dtype == np.float64}
+
+
+def _l2_note(in_bytes):
+    return ("L2 flushed between steps (256 MB write, untimed)" if in_bytes < L2_FLUSH_BELOW
+            else "inputs larger than L2 (%d MB per step), no flush" % (in_bytes >> 20))
+
+
+def _workload_metric(cfg):
+    return "%s Mpoints/s, %s: FP32-key+FP64-band vs plain FP64 on GB300" % (cfg["algorithm"].upper(),
+                                                                           cfg["workload"])
+
+
+def run_reference_workload(args):
+    """The reference arm of a non-headline workload: the oracle (OpenMP
+    restatement of coupe's Rcb/Rib, f64 weights summed in f64 in rayon-like
+    chunks as coupe does) on all host cores, each step a bounded sample."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    W = _load_workload(args.workload)
+    cfg, n = W["cfg"], W["n"]
+    kw = dict(threads=0)
+    if W["float"]:
+        kw["fsum"] = oracle.FSUM_SEQ
+    if W["batched"]:
+        groups = W["groups"]
+
+        def run(frac):
+            pts = 0
+            for d, (p, w, off, it, _) in groups.items():
+                k = max(1, int(round(len(it) * frac)))
+                m = int(off[k])
+                oracle.rcb_sets(p[:m], w[:m], off[:k + 1], it[:k], W["tol"], **kw)
+                pts += m
+            return pts
+        unit_desc = "the first sets of each dimension's batch"
+    else:
+        f = oracle.rib if W["rib"] else oracle.rcb
+
+        def run(frac):
+            m = max(1 << 16, int(n * frac)) if frac < 1.0 else n
+            f(W["pts"][:m], W["w"][:m], W["iters"], W["tol"], **kw)
+            return m
+        unit_desc = "the first points of the seeded workload"
+    t0 = time.perf_counter()
+    run(1.0 / 16)
+    t_probe = (time.perf_counter() - t0) * 16
+    frac = min(1.0, 150.0 / max(1e-9, t_probe * (args.steps + args.warmup)))
+    for _ in range(max(0, args.warmup - 1)):
+        run(frac)
+    times, done = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        done = run(frac)
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = done / (ms / 1e3) / 1e6
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": _workload_metric(cfg), "value": round(value, 3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if W["float"] else "f32",
+        "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d of %d points per step (%s); OpenMP restatement of coupe %s on all host "
+                                   "cores%s" % (done, n, unit_desc, cfg["algorithm"],
+                                                "; f64 weights summed in f64 in rayon-like chunks"
+                                                if W["float"] else "")},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_workload(args):
     """One line for a non-headline workload: every precision mode timed on
     device-resident inputs, the band form end to end from pinned host
     buffers, the top kernel's roofline and the oracle on the host cores."""
     import torch
     import coupe_gb300 as coupe
-    from coupe_gb300 import workloads
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -433,16 +539,14 @@ def run_workload(args):
     torch.cuda.set_device(dev)
     coupe.lib()
     t_gen = time.perf_counter()
-    if args.workload == "batched4096":
-        groups = workloads.batched_groups()
-        tol = 0.01
+    W = _load_workload(args.workload)
+    cfg, n, tol = W["cfg"], W["n"], W["tol"]
+    if W["batched"]:
+        groups = W["groups"]
         sets = {d: (torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev), off, it)
                 for d, (p, w, off, it, _) in groups.items()}
         hosts = {d: (p, w) for d, (p, w, _, _, _) in groups.items()}
-        n = sum(len(p) for p, _ in hosts.values())
         outs = {d: torch.empty(len(hosts[d][0]), dtype=torch.int64, device=dev) for d in sets}
-        cfg = {"workload": "batched_4096sets", "sets": 4096, "points": n, "dim": "2 and 3 (one call each)",
-               "iter_count": "U{1..8} per set", "tolerance": tol, "weights": "int64 U{1..10}"}
 
         def step(mode):
             for d, (p, w, off, it) in sets.items():
@@ -454,22 +558,19 @@ def run_workload(args):
         def cpu_run():
             return {d: oracle.rcb_sets(p, w, off, it, tol, threads=0) for d, (p, w, off, it, _) in groups.items()}
     else:
-        rib = args.workload == "hexrib134M"
-        pts_h, w_h, c = workloads.hex_mesh_rib() if rib else workloads.planes3d_lognormal()
-        iters, tol = c["iter_count"], c["tolerance"]
-        n = len(pts_h)
-        hosts = {3: (pts_h, w_h)}
+        rib = W["rib"]
+        pts_h, w_h, iters = W["pts"], W["w"], W["iters"]
+        dim = pts_h.shape[1]
+        hosts = {dim: (pts_h, w_h)}
         p_d, w_d = torch.from_numpy(pts_h).to(dev), torch.from_numpy(w_h).to(dev)
         out = torch.empty(n, dtype=torch.int64, device=dev)
-        outs = {3: out}
-        cfg = {"workload": c["name"], "points": n, "dim": 3, "parts": 1 << iters, "iter_count": iters,
-               "tolerance": tol, "weights": "float64", "algorithm": "Rib" if rib else "Rcb"}
+        outs = {dim: out}
 
         def step(mode):
             (coupe.rib_device if rib else coupe.rcb_device)(out, p_d, w_d, iters, tol, mode=mode)
 
         def ids():
-            return {3: out.cpu().numpy().view(np.uint64).copy()}
+            return {dim: out.cpu().numpy().view(np.uint64).copy()}
 
         def cpu_run():
             # the reference's arithmetic: f64 weights summed in f64, in
@@ -482,16 +583,20 @@ def run_workload(args):
             r, st = (oracle.rib if rib else oracle.rcb)(pts_h, w_h, iters, tol, **kw)
             cpu_stats.update(st)
             cpu_stats["matrix"] = kw.get("matrix")
-            return {3: r}
+            return {dim: r}
     t_gen = time.perf_counter() - t_gen
     cpu_stats = {}
     tuned = None
-    if args.workload == "batched4096":
+    if W["batched"]:
         # the schedule for this batch, picked by the library's autotuner
         # (outside the timed region; ids do not depend on it)
         p, w, off, it = sets[3]
         tuned = coupe.autotune_device(outs[3], p, w, off, it, tol, mode="f32key_f64band", repeats=1)
     stream = torch.cuda.current_stream()
+    in_bytes = sum(p.nbytes + w.nbytes for p, w in hosts.values())
+    # inputs smaller than L2 (129 MB): every timed step starts after a
+    # 256 MB write, outside its own pair of events
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev) if in_bytes < L2_FLUSH_BELOW else None
     modes = ["ref32", "f64", "f32key_f64band"]
     results, launches, got, mstats = {}, {}, {}, {}
     clocks = None
@@ -504,17 +609,24 @@ def run_workload(args):
                                            "split_steps", "max_split_steps", "algo_bytes")}
         if mode == "f32key_f64band":
             clocks = Clocks(0).__enter__()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps if flush is not None else 1)]
         nl = 0
-        ev0.record(stream)
-        for _ in range(args.steps):
+        evs[0][0].record(stream)
+        for k in range(args.steps):
+            if flush is not None:
+                flush.fill_(k & 255)
+                evs[k][0].record(stream)
             step(mode)
             nl += coupe.last_stats()["kernel_launches"]
-        ev1.record(stream)
+            if flush is not None:
+                evs[k][1].record(stream)
+        if flush is None:
+            evs[0][1].record(stream)
         torch.cuda.synchronize()
         if mode == "f32key_f64band":
             clocks.__exit__()
-        results[mode] = ev0.elapsed_time(ev1) / args.steps
+        results[mode] = sum(a.elapsed_time(b) for a, b in evs) / args.steps
         launches[mode] = nl
         got[mode] = ids()
     by_mode = {}
@@ -531,8 +643,10 @@ def run_workload(args):
     peak, peak_kind = measured_peak()
     achieved = top[1]["bytes"] / (top[1]["ms"] / 1e3) / 1e9
     roofline = {"bound": "hbm", "kernel": top[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "peak_source": peak_kind, "traffic": None,
-                "share": round(top[1]["ms"] / total_ms, 3),
+                "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                "traffic": _traffic_per_launch(top[0], "f32key_f64band", args.workload),
+                "algorithmic_bytes_per_launch": top[1]["bytes"] // max(1, top[1]["launches"]),
+                "launches": top[1]["launches"], "share": round(top[1]["ms"] / total_ms, 3),
                 "kernels": {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
                                 "share": round(v["ms"] / total_ms, 3)}
                             for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}
@@ -546,12 +660,13 @@ def run_workload(args):
         for d, (hp, hw, ho) in pins.items():
             dsts[d][0].copy_(hp, non_blocking=True)
             dsts[d][1].copy_(hw, non_blocking=True)
-        if args.workload == "batched4096":
+        if W["batched"]:
             for d, (_, _, off, it) in sets.items():
                 coupe.rcb_batched_device(outs[d], dsts[d][0], dsts[d][1], off, it, tol, mode="f32key_f64band")
         else:
-            (coupe.rib_device if args.workload == "hexrib134M" else coupe.rcb_device)(
-                outs[3], dsts[3][0], dsts[3][1], cfg["iter_count"], tol, mode="f32key_f64band")
+            d = next(iter(dsts))
+            (coupe.rib_device if W["rib"] else coupe.rcb_device)(
+                outs[d], dsts[d][0], dsts[d][1], W["iters"], tol, mode="f32key_f64band")
         for d, (_, _, ho) in pins.items():
             ho.copy_(outs[d], non_blocking=True)
         torch.cuda.synchronize()
@@ -569,16 +684,25 @@ def run_workload(args):
         t0 = time.perf_counter()
         ref = cpu_run()
         t_cpu = time.perf_counter() - t0
+        runs = [t_cpu]
+        while sum(runs) < 2.0 and len(runs) < 50:  # short runs: the median of repeats
+            t0 = time.perf_counter()
+            cpu_run()
+            runs.append(time.perf_counter() - t0)
+        t_cpu = statistics.median(runs)
         parity["ref32_vs_oracle_mismatches"] = int(sum((ref[d] != got["ref32"][d]).sum() for d in ref))
-        sample = "full workload, one run (%.2f s); OpenMP restatement of coupe %s" % (t_cpu, cfg.get("algorithm", "Rcb"))
-        if args.workload != "batched4096":
+        sample = "full workload, %s (%.3f s); OpenMP restatement of coupe %s" % (
+            "one run" if len(runs) == 1 else "median of %d runs" % len(runs), t_cpu, cfg.get("algorithm", "Rcb"))
+        if W["rib"]:
+            sample += "; given the GPU's basis change"
+        if W["float"]:
             import float_parity
-            sample += ("; f64 weights summed in f64 in rayon-like chunks (the reference's arithmetic)"
-                       + ("; given the GPU's basis change" if args.workload == "hexrib134M" else ""))
+            sample += "; f64 weights summed in f64 in rayon-like chunks (the reference's arithmetic)"
             # float-weight criteria of the GPU (REF32) against the reference's f64 sums
+            d = next(iter(hosts))
             M = cpu_stats.get("matrix")
-            keys = (oracle.map_points(hosts[3][0], M) if M is not None else hosts[3][0]).astype(np.float32)
-            crit = float_parity.compare(got["ref32"][3], ref[3], keys, hosts[3][1], cfg["iter_count"], tol,
+            keys = (oracle.map_points(hosts[d][0], M) if M is not None else hosts[d][0]).astype(np.float32)
+            crit = float_parity.compare(got["ref32"][d], ref[d], keys, hosts[d][1], W["iters"], tol,
                                         cpu_stats["split_pos"])
             crit.pop("mismatch_nodes", None)
             parity["vs_reference_f64_sums"] = crit
@@ -587,14 +711,14 @@ def run_workload(args):
     ms = results["f32key_f64band"]
     h2d = sum(p.nbytes + w.nbytes for p, w in hosts.values())
     wsum = None
-    if args.workload != "batched4096":
+    if W["float"]:
         # the run's total weight against an FP64 oracle: the exact sum (the
         # oracle's 128-bit fixed point, rounded once) and the reference's
         # chunked f64 sum
         step("f32key_f64band")
         torch.cuda.synchronize()
         st = coupe.last_stats()
-        w_h = hosts[3][1]
+        w_h = hosts[next(iter(hosts))][1]
         exact = oracle.fixed_sum(w_h, oracle.fixed_scale(w_h))
         wsum = {"gpu": st["root_weight_sum"], "exact": exact, "gpu_error": st["root_weight_sum"] - exact,
                 "gpu_error_bound": st["weight_sum_error_bound"]}
@@ -602,8 +726,7 @@ def run_workload(args):
             wsum["reference_f64"] = cpu_stats["root_sum"]
             wsum["reference_f64_error"] = cpu_stats["root_sum"] - exact
     line = {
-        "metric": "%s Mpoints/s, %s: FP32-key+FP64-band vs plain FP64 on GB300" % (
-            cfg.get("algorithm", "RCB").upper(), cfg["workload"]),
+        "metric": _workload_metric(cfg),
         "value": round(n / (ms / 1e3) / 1e6, 2), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": cfg,
@@ -634,13 +757,14 @@ def _mode_available(coupe, pts, w, part):
         return False
 
 
-def _traffic_per_launch(kernel, mode):
-    """DRAM bytes per launch of `kernel` in `mode` from the committed ncu summary."""
+def _traffic_per_launch(kernel, mode, workload="gauss16M"):
+    """DRAM bytes per launch of `kernel` in `mode` on `workload` from the
+    committed ncu summaries (profiles/traffic.json)."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(p) as f:
             t = json.load(f)
-        return t.get("%s:%s" % (mode, kernel), t.get(kernel))
+        return t.get("%s:%s:%s" % (workload, mode, kernel))
     except Exception:
         return None
 

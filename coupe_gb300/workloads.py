@@ -106,3 +106,80 @@ def hex_mesh_rib(side=512, seed=0):
     vol = 1.0 * 10.0 * 100.0
     w = vol * (1.0 + rng.random(len(pts)))
     return pts, w, dict(iter_count=10, tolerance=0.01, name="hexmesh_rib_%d^3" % side)
+
+
+def _main(argv=None):
+    """Runs one workload through the device API a few times and prints the
+    library's per-kernel CUDA-event times (the command profiles are taken
+    with):
+
+        python -m coupe_gb300.workloads gauss16M --mode f32key_f64band --runs 3
+        python -m coupe_gb300.workloads planes67M --points 16777216
+        python -m coupe_gb300.workloads hexrib134M --side 256
+        python -m coupe_gb300.workloads batched4096 --total 50000000
+        python -m coupe_gb300.workloads uniform1M
+    """
+    import argparse
+    import json
+
+    import torch
+
+    import coupe_gb300 as coupe
+    ap = argparse.ArgumentParser(prog="python -m coupe_gb300.workloads")
+    ap.add_argument("workload", choices=["uniform1M", "gauss16M", "planes67M", "batched4096", "hexrib134M"])
+    ap.add_argument("--mode", default="f32key_f64band", choices=sorted(coupe.MODES))
+    ap.add_argument("--runs", type=int, default=3)
+    ap.add_argument("--points", type=int, default=None, help="points (uniform1M, gauss16M, planes67M)")
+    ap.add_argument("--side", type=int, default=512, help="hex mesh side (hexrib134M)")
+    ap.add_argument("--sets", type=int, default=4096, help="sets (batched4096)")
+    ap.add_argument("--total", type=int, default=200_000_000, help="about this many points (batched4096)")
+    a = ap.parse_args(argv)
+    dev = torch.device("cuda", 0)
+    kw = {} if a.points is None else {"n": a.points}
+    if a.workload == "batched4096":
+        groups = batched_groups(a.sets, 0, a.total)
+        calls = []
+        for d, (p, w, off, it, _) in groups.items():
+            dp, dw = torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev)
+            out = torch.empty(len(p), dtype=torch.int64, device=dev)
+            calls.append(lambda out=out, dp=dp, dw=dw, off=off, it=it:
+                         coupe.rcb_batched_device(out, dp, dw, off, it, 0.01, mode=a.mode))
+        n = sum(len(g[0]) for g in groups.values())
+    else:
+        gen = {"uniform1M": uniform2d_unit, "gauss16M": gaussian_mixture3d, "planes67M": planes3d_lognormal}
+        if a.workload == "hexrib134M":
+            p, w, c = hex_mesh_rib(side=a.side)
+        else:
+            p, w, c = gen[a.workload](**kw)
+        dp, dw = torch.from_numpy(p).to(dev), torch.from_numpy(w).to(dev)
+        out = torch.empty(len(p), dtype=torch.int64, device=dev)
+        f = coupe.rib_device if a.workload == "hexrib134M" else coupe.rcb_device
+        calls = [lambda: f(out, dp, dw, c["iter_count"], c["tolerance"], mode=a.mode)]
+        n = len(p)
+    for call in calls:  # warm-up (workspace, autotune cache)
+        call()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(a.runs):
+        for call in calls:
+            call()
+    ev1.record()
+    torch.cuda.synchronize()
+    coupe.profile(True)
+    for _ in range(a.runs):
+        for call in calls:
+            call()
+    torch.cuda.synchronize()
+    prof = coupe.profile_read()
+    coupe.profile(False)
+    print(json.dumps({"workload": a.workload, "points": n, "mode": a.mode, "runs": a.runs,
+                      "ms_per_run": round(ev0.elapsed_time(ev1) / a.runs, 4),
+                      "kernels": {k: {"launches_per_run": v["launches"] / a.runs,
+                                      "us_per_run": round(1e3 * v["ms"] / a.runs, 1),
+                                      "algorithmic_bytes_per_launch": v["bytes"] // max(1, v["launches"])}
+                                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}}))
+
+
+if __name__ == "__main__":
+    _main()

@@ -231,3 +231,50 @@ def test_batched_sharded_over_ranks(tmp_path):
     out = str(tmp_path / "ok.npy")
     mp.start_processes(_batched_worker, args=(2, _free_port(), out), nprocs=2, start_method="spawn")
     assert np.load(out).all()
+
+
+def _failing_worker(rank, world, port, out_dir):
+    """Rank 1's fold raises on its first call; rank 0 must see its next
+    collective end with an error (the peer is gone) instead of waiting."""
+    import datetime
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=10))
+    status = "finished"
+    try:
+        rng = np.random.default_rng(5)
+        n = 4000
+        pts = rng.random((n, 2))
+        w = rng.integers(1, 100, size=n, dtype=np.int64)
+        mine = np.arange(rank, n, world)
+
+        def fold(k, ww, t):
+            if rank == 1:
+                raise RuntimeError("injected failure in rank 1's fold")
+            return fold_int(k, ww, t)
+        algo = D.SingleSetRcb(dist.group.WORLD, fold, make_local_rcb(fold_int, False), False)
+        algo.partition(pts[mine].astype(F32), w[mine], mine.astype(np.int64), n, 4, 0.01,
+                       (pts.min(axis=0).tolist(), pts.max(axis=0).tolist()))
+    except Exception as e:  # recorded for the test, then the rank leaves
+        status = "error: %s: %s" % (type(e).__name__, str(e)[:200])
+    finally:
+        with open(os.path.join(out_dir, "rank%d.txt" % rank), "w") as f:
+            f.write(status)
+        if rank == 1:
+            os._exit(0)  # leave without a clean shutdown, as a crashed rank does
+        try:
+            dist.destroy_process_group()
+        except Exception:
+            pass
+
+
+def test_failing_rank_ends_the_others_collectives(tmp_path):
+    """A rank that fails between collectives (host-side failure, no GPU):
+    its error is its own, and the surviving rank's next all-reduce ends with
+    an error within the group's timeout instead of hanging."""
+    mp.start_processes(_failing_worker, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True,
+                       start_method="spawn")
+    r1 = open(tmp_path / "rank1.txt").read()
+    r0 = open(tmp_path / "rank0.txt").read()
+    assert r1.startswith("error: RuntimeError: injected failure"), r1
+    assert r0.startswith("error:"), r0

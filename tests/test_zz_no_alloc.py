@@ -6,6 +6,7 @@ of the session (the split's static scratch then follows other calls on the
 same device); it passes alone in a fresh process too.
 """
 import ctypes
+import gc
 
 import numpy as np
 import pytest
@@ -131,12 +132,20 @@ def test_split_allocates_nothing(coupe):
                  ctypes.byref(nl), s)
     assert call() == ERR_OK  # set-up on this device (if not done already)
     torch.cuda.synchronize()
-    free0, _ = torch.cuda.mem_get_info()
-    alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
-    for _ in range(3):
-        assert call() == ERR_OK
-    torch.cuda.synchronize()
-    free1, _ = torch.cuda.mem_get_info()
+    # tensors of earlier tests that only a garbage collection frees would
+    # change torch's counters in the middle of the measurement
+    gc.collect()
+    gc.disable()
+    try:
+        free0, _ = torch.cuda.mem_get_info()
+        alloc0, reserved0 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+        for _ in range(3):
+            assert call() == ERR_OK
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        alloc1, reserved1 = torch.cuda.memory_allocated(), torch.cuda.memory_reserved()
+    finally:
+        gc.enable()
     assert free1 == free0
-    assert torch.cuda.memory_allocated() == alloc0 and torch.cuda.memory_reserved() == reserved0
+    assert alloc1 == alloc0 and reserved1 == reserved0
     assert nl.value == int((dp[:, 1] < 0.5).sum().item())
