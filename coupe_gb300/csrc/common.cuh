@@ -525,6 +525,7 @@ enum : uint32_t {
     ERR_NONFINITE_WEIGHT = 4u,
     ERR_COUNT_MISMATCH = 8u,
     ERR_TILE_PERM = 16u,  // a reorder tile's permutation left its range
+    ERR_COPY_TIMEOUT = 32u,  // a bulk copy into shared memory did not complete within its bounded wait
 };
 
 // Device-side scalars of one run.

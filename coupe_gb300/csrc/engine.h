@@ -49,6 +49,7 @@ struct Tuning {
     int reorder_chunks_per_cta = 1;  // reorder chunks per resident CTA
     int hist_ctas_per_sm = 0;        // histogram CTAs per SM (0: as many as fit)
     int exact_f64_hist = 0;          // 1: f64 weights always binned exactly
+    int reorder_kernel = 0;          // 0: by segment size; 1: k_reorder (bulk copies); 2: k_reorder_small
     // Failure handling (not scheduling): polls of a reorder chunk's bounded
     // look-back wait before it gives up with an error, and a cap on the
     // engine workspace in MiB (0: none; a run needing more fails with

@@ -925,6 +925,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
     if (!std::strcmp(name, "hist_ctas_per_sm")) return &t.hist_ctas_per_sm;
     if (!std::strcmp(name, "exact_f64_hist")) return &t.exact_f64_hist;
+    if (!std::strcmp(name, "reorder_kernel")) return &t.reorder_kernel;
     if (!std::strcmp(name, "lookback_spin_limit")) return &t.lookback_spin_limit;
     if (!std::strcmp(name, "workspace_limit_mb")) return &t.workspace_limit_mb;
     if (!std::strcmp(name, "sync_levels")) return &t.sync_levels;

@@ -243,6 +243,57 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// Bulk copies between global and shared memory (the copy engine behind TMA,
+// one-dimensional form: no tensor map).  A load is issued by one thread and
+// completes on an mbarrier that counts its bytes; a store reads shared
+// memory asynchronously, tracked by bulk groups.  Addresses and sizes are
+// multiples of 16 bytes.  Shared memory written by threads must be fenced
+// into the async proxy before a bulk store reads it, and shared memory read
+// by threads before a bulk load overwrites it.
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t arrivals) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(arrivals) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+// true once the phase with parity `phase` has completed (the call itself
+// may suspend the thread for a short, bounded time)
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+// waits at most `limit` polls; false when the phase did not complete
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t phase, uint32_t limit) {
+    for (uint32_t i = 0; i <= limit; ++i)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+__device__ __forceinline__ void bulk_load(void *dst_smem, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_addr(dst_smem)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_store(void *dst, const void *src_smem, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n" ::"l"(dst), "r"(smem_addr(src_smem)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;\n" ::: "memory"); }
+// the committed bulk stores have read their shared memory
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory"); }
+// the committed bulk stores have completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+
 struct Mat {
     double m[9];
     int on;
@@ -2158,10 +2209,15 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
 // place, one dynamic chunk of the item range per CTA at a time.  A chunk
 // learns how many left items of its first segment precede it by a decoupled
 // look-back over the chunks before it (bounded wait).  The chunk is walked in
-// tiles of R_TILE items staged in shared memory by asynchronous copies (the
-// next tile lands while the current one is partitioned); each tile is
-// permuted in shared memory and leaves as two coalesced runs, its left items
-// and its right items.
+// tiles; a tile arrives in shared memory by bulk copies (one per array,
+// issued by one thread, completing on an mbarrier).  Every thread scatters
+// its items into an output stage, the tile's left run then its right run,
+// each placed at the alignment phase of its destination; once the stage is
+// complete the next tile's copies are issued, and each run leaves by one bulk
+// store per array (its 16-byte-aligned middle) plus plain stores of its few
+// unaligned end elements.  One input buffer and one stage per CTA keep the
+// shared memory small enough for three or four CTAs per SM, which hide the
+// copies' latency better than a second buffer in fewer CTAs (measured).
 // ---------------------------------------------------------------------------
 template <int D, class KT, class WT>
 struct ReorderArgs {
@@ -2186,31 +2242,50 @@ struct ReorderArgs {
     const uint64_t *n_ptr;
 };
 
-// One tile in shared memory: D key arrays and a weight array, each with 16
-// bytes of slack.  Arrays in engine buffers (keys, and weights after level 0)
-// arrive as the 16-byte chunks covering the tile, starting at the aligned
-// address at or below it; element li of the tile is then at li + head, head =
-// ts mod (16 / element size).  Carried input indices are not double
-// buffered: each thread loads its own items' indices into registers when the
-// tile starts (overlapping the partition work) and parks them in one shared
-// array for the output loop.
-template <int D, class KT>
-__host__ __device__ constexpr size_t reorder_key_stride() {
-    return (size_t)R_TILE * sizeof(typename KT::T) + 16;
+// Items per thread per tile: 8 (2048 per tile) when an item moves at most 18
+// bytes (then three CTAs' tiles and stages fit an SM's shared memory), else
+// 4; and the CTAs per SM the registers are bounded for: four with 4-byte
+// keys and 4 items, else three.
+template <int D, class KT, class WT, bool IDX>
+__host__ __device__ constexpr int reorder_items() {
+    return D * sizeof(typename KT::T) + sizeof(typename WT::S) + (IDX ? 4 : 0) <= 18 ? 8 : 4;
 }
-template <int D, class KT, class WT>
-__host__ __device__ constexpr size_t reorder_tile_bytes() {
-    return D * reorder_key_stride<D, KT>() + (size_t)R_TILE * sizeof(typename WT::S) + 16;
+template <int D, class KT, class WT, bool IDX>
+__host__ __device__ constexpr int reorder_min_ctas() {
+    return reorder_items<D, KT, WT, IDX>() == 4 && sizeof(typename KT::T) == 4 ? 4 : 3;
 }
+__host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-// Dynamic shared memory of the reorder: two tiles (asynchronous double
-// buffering), the tile's inverse permutation and, when indices are carried,
-// the tile's indices.
+// Dynamic shared memory of the reorder, in 16-byte-aligned arrays:
+//   the input tile: D key arrays, the weights and (IDX) the input indices;
+//   array a holds the 16-byte chunks covering the tile from the
+//   aligned address at or below it (element li at head + li, head = ts mod
+//   16 / element size), so RT elements and 16 bytes;
+//   one output stage with the same arrays of RT + 24 elements: the left run
+//   starts at element (left destination mod 8) and the right run at the next
+//   element after it with the right destination's phase mod 8.
+template <int D, class KT, class WT, bool IDX>
+struct ReorderSmem {
+    static constexpr int RT = BLOCK * reorder_items<D, KT, WT, IDX>();
+    static constexpr size_t KS = sizeof(typename KT::T), WSZ = sizeof(typename WT::S);
+    static constexpr size_t in_key = al16(RT * KS + 16);
+    static constexpr size_t in_w = al16(RT * WSZ + 16);
+    static constexpr size_t in_idx = IDX ? al16(RT * 4 + 16) : 0;
+    static constexpr size_t in_tile = D * in_key + in_w + in_idx;
+    static constexpr int OE = RT + 24;
+    static constexpr size_t out_key = al16(OE * KS);
+    static constexpr size_t out_w = al16(OE * WSZ);
+    static constexpr size_t out_idx = IDX ? al16(OE * 4) : 0;
+    static constexpr size_t out_tile = D * out_key + out_w + out_idx;
+    static constexpr size_t bytes = in_tile + out_tile;
+};
 template <int D, class KT, class WT>
 __host__ __device__ constexpr size_t reorder_smem(bool with_index) {
-    return 2 * reorder_tile_bytes<D, KT, WT>() + (size_t)R_TILE * sizeof(uint16_t) +
-           (with_index ? (size_t)R_TILE * sizeof(uint32_t) : 0);
+    return with_index ? ReorderSmem<D, KT, WT, true>::bytes : ReorderSmem<D, KT, WT, false>::bytes;
 }
+// polls of an input tile's mbarrier before the reorder gives up (the copies
+// of a tile take microseconds; this is a guard, not a schedule)
+constexpr uint32_t MBAR_SPIN_LIMIT = 1u << 22;
 
 template <class KT>
 __device__ __forceinline__ bool goes_left(typename KT::T key, const Seg<KT> &sg) {
@@ -2234,17 +2309,470 @@ struct TileRef {
     bool valid;
 };
 
+// One run of a tile (len elements from stage element S on) to dst[G ..), by
+// the first warp: the 16-byte-aligned middle [j0, j1) by one bulk store (lane
+// 0), the elements before and after it by plain stores (lanes 0-15 and
+// 16-23).  S has the
+// phase of G mod 8 elements, so the middle is aligned on both sides.  A run
+// without a whole aligned 16-byte block is all head (j0 = j1 = len < 16).
+template <class E>
+__device__ __forceinline__ void put_run(E *dst, const E *stg, uint64_t G, uint32_t S, uint32_t len, uint32_t cap,
+                                        uint32_t *err) {
+    if (S + len > cap) {  // a run past the stage: write nothing
+        if (threadIdx.x == 0) atomicOr(err, ERR_TILE_PERM);
+        return;
+    }
+    constexpr uint64_t m = 16 / sizeof(E) - 1;
+    const uint64_t a0 = (G + m) & ~m;    // first aligned element at or after G
+    const uint64_t a1 = (G + len) & ~m;  // last aligned element at or before the end
+    uint32_t j0 = len, j1 = len;
+    if (a1 > a0) {
+        j0 = (uint32_t)(a0 - G);  // <= m
+        j1 = (uint32_t)(a1 - G);  // len - j1 <= m
+    }
+    if (threadIdx.x == 0 && j1 > j0) bulk_store(dst + G + j0, stg + S + j0, (j1 - j0) * (uint32_t)sizeof(E));
+    const uint32_t t = threadIdx.x;
+    if (t < j0)
+        dst[G + t] = stg[S + t];
+    else if (t >= 16 && t - 16 < len - j1)
+        dst[G + j1 + (t - 16)] = stg[S + j1 + (t - 16)];
+}
+
+// The number of keys kc[la, le) that go left, by the whole CTA: side(k) is
+// -1 (left), 1 (right) or 0 (undecided by the key: the band form's f64
+// check), and exact(e) decides item e then.  16-byte loads, four in flight
+// per thread (16 KB per CTA), after a scalar head up to the first 16-byte
+// boundary; the count is on the chunk's look-back chain, so its loads are
+// kept in flight together, and the rare exact checks (a call) run after the
+// keys of an iteration are no longer needed.
+template <class K, class SideFn, class ExactFn>
+__device__ __forceinline__ uint64_t count_left_keys(const K *__restrict__ kc, uint64_t la, uint64_t le, SideFn side,
+                                                    ExactFn exact) {
+    constexpr uint64_t V = 16 / sizeof(K);  // keys per 16 bytes
+    uint64_t cnt = 0;
+    auto one = [&](K k, uint64_t e) {
+        const int sd = side(k);
+        cnt += sd < 0 ? 1u : (sd == 0 ? exact(e) : 0u);
+    };
+    uint64_t a = (la + V - 1) & ~(V - 1);
+    if (a > le) a = le;
+    for (uint64_t e = la + threadIdx.x; e < a; e += BLOCK) one(kc[e], e);
+    const uint64_t nq = (le - a) / V;  // whole 16-byte groups
+    const uint4 *q4 = (const uint4 *)(kc + a);
+    uint64_t q = threadIdx.x;
+    for (; q + 3 * BLOCK < nq; q += 4 * BLOCK) {
+        uint4 v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = q4[q + j * BLOCK];
+        uint32_t und = 0;  // bit j * V + i: key i of load j is undecided
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const K *kk = (const K *)&v[j];
+#pragma unroll
+            for (int i = 0; i < (int)V; ++i) {
+                const int sd = side(kk[i]);
+                cnt += sd < 0 ? 1u : 0u;
+                und |= (sd == 0 ? 1u : 0u) << (j * V + i);
+            }
+        }
+        while (und) {
+            const int b = __ffs(und) - 1;
+            und &= und - 1;
+            cnt += exact(a + (q + (b / V) * BLOCK) * V + (b % V));
+        }
+    }
+    for (; q < nq; q += BLOCK) {
+        const uint4 v = q4[q];
+        const K *kk = (const K *)&v;
+        const uint64_t e = a + q * V;
+#pragma unroll
+        for (int i = 0; i < (int)V; ++i) one(kk[i], e + i);
+    }
+    for (uint64_t e = a + nq * V + threadIdx.x; e < le; e += BLOCK) one(kc[e], e);
+    return cnt;
+}
+
+// IDX: the reorder also carries input indices (isrc -> idst); a compile-time
+// choice, so that reorders without indices spend no shared memory or
+// registers on them.
+template <int D, class KT, class WT, bool IDX>
+__global__ void __launch_bounds__(BLOCK, (reorder_min_ctas<D, KT, WT, IDX>())) k_reorder(ReorderArgs<D, KT, WT> A) {
+    typedef typename KT::T K;
+    typedef typename WT::S WS;
+    typedef ReorderSmem<D, KT, WT, IDX> SM;
+    constexpr int RI = reorder_items<D, KT, WT, IDX>();
+    constexpr uint32_t RT = SM::RT;
+    extern __shared__ __align__(16) unsigned char dsm[];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_cnt[RI * NWARPS];
+    __shared__ uint64_t sh[33];
+    __shared__ uint64_t s_ticket, s_prefix;
+    __shared__ uint32_t s_fail;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const K *__restrict__ kc = A.coord == 0 ? A.ksrc[0] : (A.coord == 1 ? A.ksrc[1] : A.ksrc[2]);
+    auto in_key = [&](int d) { return (K *)(dsm + d * SM::in_key); };
+    WS *const in_w = (WS *)(dsm + D * SM::in_key);
+    uint32_t *const in_idx = (uint32_t *)(dsm + D * SM::in_key + SM::in_w);
+    unsigned char *const ob = dsm + SM::in_tile;
+    auto out_key = [&](int d) { return (K *)(ob + d * SM::out_key); };
+    WS *const out_w = (WS *)(ob + D * SM::out_key);
+    uint32_t *const out_idx = (uint32_t *)(ob + D * SM::out_key + SM::out_w);
+    constexpr uint64_t KMASK = 16 / sizeof(K) - 1, WMASK = 16 / sizeof(WS) - 1, IMASK = 3;
+    // engine buffers are copied in bulk; the caller's weights (level 0) and
+    // the identity indices of level 0 are read or made per item
+    const bool w_bulk = A.wsafe != 0;
+    const bool i_bulk = IDX && A.isrc != nullptr;
+
+    if (cta_halted(A.rs)) return;
+    if (threadIdx.x == 0) {
+        mbar_init(&s_bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;     // parity of the input tile's next mbarrier phase
+    bool inflight = false;  // a tile load issued and not yet waited for (same in every thread)
+
+    // thread 0: the bulk loads of tile t
+    auto load_tile = [&](const TileRef &t) {
+        const uint64_t k0 = t.ts & ~KMASK;
+        const uint32_t kbytes = (uint32_t)(((t.te - k0) * sizeof(K) + 15) & ~15ull);
+        uint32_t total = D * kbytes;
+        uint64_t w0 = 0, i0 = 0;
+        uint32_t wbytes = 0, ibytes = 0;
+        if (w_bulk) {
+            w0 = t.ts & ~WMASK;
+            wbytes = (uint32_t)(((t.te - w0) * sizeof(WS) + 15) & ~15ull);
+            total += wbytes;
+        }
+        if (i_bulk) {
+            i0 = t.ts & ~IMASK;
+            ibytes = (uint32_t)(((t.te - i0) * 4 + 15) & ~15ull);
+            total += ibytes;
+        }
+        mbar_arrive_expect_tx(&s_bar, total);
+#pragma unroll
+        for (int d = 0; d < D; ++d) bulk_load(in_key(d), A.ksrc[d] + k0, kbytes, &s_bar);
+        if (w_bulk) bulk_load(in_w, A.wsrc + w0, wbytes, &s_bar);
+        if (i_bulk) bulk_load(in_idx, A.isrc + i0, ibytes, &s_bar);
+    };
+    // every thread: wait for the tile (bounded); false (in every thread)
+    // when a wait ran out
+    auto wait_tile = [&]() -> bool {
+        const bool ok = mbar_wait_bounded(&s_bar, phase, MBAR_SPIN_LIMIT);
+        const bool all = __syncthreads_and(ok) != 0;
+        if (all) {
+            phase ^= 1u;
+            inflight = false;
+        }
+        return all;
+    };
+    // a wait ran out: record it, give the copies in flight one more bounded
+    // wait, let the bulk stores finish, and leave
+    auto give_up = [&]() {
+        if (threadIdx.x == 0) {
+            atomicOr(&A.rs->err, ERR_COPY_TIMEOUT);
+            if (inflight) mbar_wait_bounded(&s_bar, phase, MBAR_SPIN_LIMIT);
+            bulk_wait_all();
+        }
+        __syncthreads();
+    };
+
+    // the level's counts from the device when the host queued the level
+    // without them (chunks of the host's size over the actual items); kept
+    // in locals: writing to the parameter struct would copy it to local
+    // memory
+    const uint32_t A_S = A.S_ptr ? (uint32_t)*A.S_ptr : A.S;
+    const uint64_t A_n = A.n_ptr ? *A.n_ptr : A.n;
+    const uint64_t A_nchunks = A.n_ptr ? (A_n + A.chunk - 1) / A.chunk : A.nchunks;
+    for (;;) {
+        if (threadIdx.x == 0) s_ticket = atomicAdd((unsigned long long *)&A.rs->ticket, 1ull);
+        __syncthreads();
+        const uint64_t t = s_ticket;
+        if (t >= A_nchunks) break;
+        // [c0, c1): positions in the list of the level's items; a segment's
+        // items are at off + (position - voff)
+        const uint64_t c0 = t * A.chunk, c1 = min(A_n, c0 + A.chunk);
+        const uint32_t kf = seg_index_of_v<KT>(A.segs, A_S, c0);
+        const uint32_t kl = seg_index_of_v<KT>(A.segs, A_S, c1 - 1);
+        auto piece_end = [&](const Seg<KT> &g) { return g.off + (min(c1, g.voff + g.n) - g.voff); };
+        const Seg<KT> sf = A.segs[kf];
+        TileRef cur;
+        cur.kk = kf;
+        cur.ts = sf.off + (c0 - sf.voff);
+        cur.pend = piece_end(sf);
+        cur.te = min(cur.ts + RT, cur.pend);
+        cur.first = true;
+        cur.valid = true;
+        if (threadIdx.x == 0) load_tile(cur);  // overlaps the count below
+        inflight = true;
+        // count the left items of the last piece
+        const Seg<KT> sl = A.segs[kl];
+        const uint64_t la = sl.off + (max(c0, sl.voff) - sl.voff), le = sl.off + (c1 - sl.voff);
+        uint64_t cnt = 0;
+        {
+            CutBounds spb = {0.f, 0.f};
+            if constexpr (KT::BAND) spb = band_bounds(sl.pivot);
+            auto side = [&](K k) -> int {
+                if constexpr (KT::BAND)
+                    return sl.state == SEG_ALLLEFT ? -1 : band_side(k, spb);
+                else
+                    return goes_left<KT>(k, sl) ? -1 : 1;
+            };
+            auto exact = [&](uint64_t e) -> uint32_t {
+                return KeyF64::lt(band_code_cold(&A.bs, A.isrc ? A.isrc[e] : e, A.coord), sl.pivot) ? 1u : 0u;
+            };
+            cnt = count_left_keys<K>(kc, la, le, side, exact);
+        }
+        uint64_t agg;
+        block_exscan_u64(cnt, sh, agg);
+        if (threadIdx.x == 0) {
+            const bool last_starts_here = sl.voff >= c0;
+            s_fail = 0;
+            if (last_starts_here) atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_INCL | agg));
+            else atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_AGG | agg));
+            uint64_t prefix = 0;
+            if (sf.voff < c0) {
+                // look back: chunk t-1 ends inside segment kf
+                int64_t j = (int64_t)t - 1;
+                for (;;) {
+                    uint64_t v;
+                    uint32_t spins = 0;
+                    while ((v = *((volatile uint64_t *)&A.lb[j])) == 0) {
+                        if (++spins > A.spin_limit) break;
+                        __nanosleep(64);
+                    }
+                    if (v == 0) {
+                        atomicOr(&A.rs->err, ERR_LOOKBACK_TIMEOUT);
+                        s_fail = 1;
+                        break;
+                    }
+                    prefix += v & LB_VALUE;
+                    if ((v & ~LB_VALUE) == LB_INCL) break;
+                    if (--j < 0) {
+                        atomicOr(&A.rs->err, ERR_LOOKBACK_TIMEOUT);
+                        s_fail = 1;
+                        break;
+                    }
+                }
+                if (!last_starts_here)
+                    atomicExch((unsigned long long *)&A.lb[t], (unsigned long long)(LB_INCL | ((prefix + agg) & LB_VALUE)));
+            }
+            s_prefix = prefix;
+        }
+        __syncthreads();
+        if (s_fail) {
+            // the chunk writes nothing; its tile must land before the buffer is reused
+            if (!wait_tile()) {
+                give_up();
+                return;
+            }
+            continue;
+        }
+        const uint64_t prefix_first = s_prefix;
+        // the current piece's segment, as scalars (kept in registers rather
+        // than re-read from the segment table)
+        uint64_t p_off = 0, p_nleft = 0;
+        uint32_t p_state = 0;
+        typename KT::C p_pivot = 0;
+        CutBounds pb = {0.f, 0.f};  // band form: bounds of p_pivot
+        uint64_t running = 0, seg_end = 0, left_end = 0;
+        while (cur.valid) {
+            // the next tile of the chunk (it may start the next segment); the
+            // segment table is read once per piece, here
+            TileRef nxt;
+            nxt.valid = false;
+            if (cur.te < cur.pend) {
+                nxt.kk = cur.kk;
+                nxt.ts = cur.te;
+                nxt.pend = cur.pend;
+                nxt.first = false;
+                nxt.valid = true;
+            } else if (cur.kk < kl) {
+                nxt.kk = cur.kk + 1;
+                const Seg<KT> &g = A.segs[nxt.kk];
+                nxt.ts = g.off;
+                nxt.pend = piece_end(g);
+                nxt.first = true;
+                nxt.valid = true;
+            }
+            if (nxt.valid) nxt.te = min(nxt.ts + RT, nxt.pend);
+            if (!wait_tile()) {
+                give_up();
+                return;
+            }
+            if (cur.first) {
+                const Seg<KT> &g = A.segs[cur.kk];
+                p_off = g.off;
+                p_nleft = g.nleft;
+                p_state = g.state;
+                p_pivot = g.pivot;
+                if constexpr (KT::BAND) pb = band_bounds(p_pivot);
+                running = cur.kk == kf ? prefix_first : 0;
+                seg_end = p_off + g.n;
+                left_end = p_off + p_nleft;
+            }
+            const uint32_t tcount = (uint32_t)(cur.te - cur.ts);
+            const uint32_t kh = (uint32_t)(cur.ts & KMASK);
+            const uint32_t wh = (uint32_t)(cur.ts & WMASK);
+            const uint32_t ih = (uint32_t)(cur.ts & IMASK);
+            const K *tkc = in_key(A.coord) + kh;
+            // input index of the tile's item li (level 0: the identity)
+            auto orig_of = [&](uint32_t li) -> uint32_t { return i_bulk ? in_idx[ih + li] : (uint32_t)(cur.ts + li); };
+            bool fl[RI];
+            uint32_t bal[RI];
+#pragma unroll
+            for (int i = 0; i < RI; ++i) {
+                const uint32_t li = i * BLOCK + threadIdx.x;
+                if constexpr (KT::BAND)
+                    fl[i] = li < tcount &&
+                            (p_state == SEG_ALLLEFT || band_side(tkc[li], pb) < 0 ||
+                             (band_side(tkc[li], pb) == 0 &&
+                              KeyF64::lt(band_code_cold(&A.bs, orig_of(li), A.coord), p_pivot)));
+                else
+                    fl[i] = li < tcount && (p_state == SEG_ALLLEFT || KT::lt(tkc[li], p_pivot));
+                bal[i] = __ballot_sync(0xffffffffu, fl[i]);
+                if (lane == 0) s_cnt[i * NWARPS + warp] = __popc(bal[i]);
+            }
+            __syncthreads();
+            if (warp == 0) {
+                // exclusive scan of RI * NWARPS counts in (row, warp) order
+                constexpr int PER = (RI * NWARPS + 31) / 32;
+                uint32_t v[PER], tot = 0;
+#pragma unroll
+                for (int j = 0; j < PER; ++j) {
+                    const int idx = lane * PER + j;
+                    v[j] = idx < RI * NWARPS ? s_cnt[idx] : 0;
+                    tot += v[j];
+                }
+                uint32_t inc = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (lane >= o) inc += u;
+                }
+                uint32_t run = inc - tot;
+#pragma unroll
+                for (int j = 0; j < PER; ++j) {
+                    const int idx = lane * PER + j;
+                    if (idx < RI * NWARPS) s_cnt[idx] = run;
+                    run += v[j];
+                }
+                if (lane == 31) sh[0] = inc;
+                if (lane == 0) bulk_wait_read_all();  // the last tile's bulk stores have read the stage
+            }
+            __syncthreads();
+            const uint32_t tile_left = (uint32_t)sh[0];
+            // both runs are checked against the segment once per tile
+            const uint64_t left_base = p_off + running;
+            const uint64_t right_base = p_off + p_nleft + (cur.ts - p_off - running);
+            const bool runs_ok = tile_left <= tcount && left_base + tile_left <= left_end && right_base >= left_end &&
+                                 right_base + (tcount - tile_left) <= seg_end;
+            if (!runs_ok && threadIdx.x == 0) atomicOr(&A.rs->err, ERR_SCATTER_BOUNDS);
+            // stage elements of the two runs
+            const uint32_t SL = (uint32_t)(left_base & 7);
+            const uint32_t SR = ((SL + tile_left + 7) & ~7u) + (uint32_t)(right_base & 7);
+            if (runs_ok) {
+                const K *ik[D];
+                K *ok[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    ik[d] = in_key(d) + kh;
+                    ok[d] = out_key(d);
+                }
+                const WS *iw = w_bulk ? in_w + wh : A.wsrc + cur.ts;  // the caller's weights: read in place
+                const uint32_t *ii = in_idx + ih;
+                const uint32_t lmask = (1u << lane) - 1;
+#pragma unroll
+                for (int i = 0; i < RI; ++i) {
+                    const uint32_t li = i * BLOCK + threadIdx.x;
+                    if (li >= tcount) continue;
+                    const uint32_t before = s_cnt[i * NWARPS + warp] + __popc(bal[i] & lmask);
+                    // a rank outside its run would write past the stage: skip it
+                    if (fl[i] ? before >= tile_left : li - before >= tcount - tile_left) {
+                        atomicOr(&A.rs->err, ERR_TILE_PERM);
+                        continue;
+                    }
+                    const uint32_t pos = fl[i] ? SL + before : SR + (li - before);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) ok[d][pos] = ik[d][li];
+                    out_w[pos] = iw[li];
+                    if constexpr (IDX) out_idx[pos] = i_bulk ? ii[li] : (uint32_t)(cur.ts + li);
+                }
+            }
+            fence_proxy_async_smem();  // the stage's writes (and the tile's reads), before the bulk copies
+            __syncthreads();           // the stage is complete and the input tile free
+            if (nxt.valid) {
+                if (threadIdx.x == 0) load_tile(nxt);
+                inflight = true;
+            }
+            if (runs_ok && warp == 0) {
+                const uint32_t nr = tcount - tile_left;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    put_run<K>(A.kdst[d], out_key(d), left_base, SL, tile_left, SM::OE, &A.rs->err);
+                    put_run<K>(A.kdst[d], out_key(d), right_base, SR, nr, SM::OE, &A.rs->err);
+                }
+                put_run<WS>(A.wdst, out_w, left_base, SL, tile_left, SM::OE, &A.rs->err);
+                put_run<WS>(A.wdst, out_w, right_base, SR, nr, SM::OE, &A.rs->err);
+                if constexpr (IDX) {
+                    put_run<uint32_t>(A.idst, out_idx, left_base, SL, tile_left, SM::OE, &A.rs->err);
+                    put_run<uint32_t>(A.idst, out_idx, right_base, SR, nr, SM::OE, &A.rs->err);
+                }
+                if (threadIdx.x == 0) bulk_commit();
+            }
+            running += tile_left;
+            cur = nxt;
+        }
+    }
+    if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// ---------------------------------------------------------------------------
+// k_reorder_small: the same partition for levels whose segments are smaller
+// than a few tiles (the batched form's deep levels).  A piece of such a
+// segment is one short tile, and k_reorder's single input buffer would wait
+// for every tile's copies in turn; here two tile buffers are filled by
+// per-thread asynchronous copies (cp.async), so the next piece's tile lands
+// while the current one is partitioned.  The tile is permuted in shared
+// memory (a 16-bit slot -> item table) and leaves as two coalesced runs.
+// ---------------------------------------------------------------------------
+// One tile in shared memory: D key arrays and a weight array, each with 16
+// bytes of slack.  Arrays in engine buffers (keys, and weights after level 0)
+// arrive as the 16-byte chunks covering the tile, starting at the aligned
+// address at or below it; element li of the tile is then at li + head, head =
+// ts mod (16 / element size).  Carried input indices are not double
+// buffered: each thread loads its own items' indices into registers when the
+// tile starts (overlapping the partition work) and parks them in one shared
+// array for the output loop.
+template <int D, class KT>
+__host__ __device__ constexpr size_t small_reorder_key_stride() {
+    return (size_t)R_TILE * sizeof(typename KT::T) + 16;
+}
+template <int D, class KT, class WT>
+__host__ __device__ constexpr size_t small_reorder_tile_bytes() {
+    return D * small_reorder_key_stride<D, KT>() + (size_t)R_TILE * sizeof(typename WT::S) + 16;
+}
+
+// Dynamic shared memory of the reorder: two tiles (asynchronous double
+// buffering), the tile's inverse permutation and, when indices are carried,
+// the tile's indices.
+template <int D, class KT, class WT>
+__host__ __device__ constexpr size_t small_reorder_smem(bool with_index) {
+    return 2 * small_reorder_tile_bytes<D, KT, WT>() + (size_t)R_TILE * sizeof(uint16_t) +
+           (with_index ? (size_t)R_TILE * sizeof(uint32_t) : 0);
+}
+
 // IDX: the reorder also carries input indices (isrc -> idst); a compile-time
 // choice, so that reorders without indices spend no registers on them.  With
 // 4-byte keys three CTAs fit an SM's shared memory; the bound keeps the
 // registers within that too.
 template <int D, class KT, class WT, bool IDX>
-__global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_reorder(ReorderArgs<D, KT, WT> A) {
+__global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_reorder_small(ReorderArgs<D, KT, WT> A) {
     typedef typename KT::T K;
     typedef typename WT::S WS;
     extern __shared__ __align__(16) unsigned char dsm[];
     constexpr bool with_index = IDX;
-    const size_t tile_bytes = reorder_tile_bytes<D, KT, WT>();
+    const size_t tile_bytes = small_reorder_tile_bytes<D, KT, WT>();
     uint16_t *perm = (uint16_t *)(dsm + 2 * tile_bytes);  // tile slot -> item of the tile
     uint32_t *s_idx = (uint32_t *)(perm + R_TILE);          // carried indices of the tile (item order)
     __shared__ uint32_t s_cnt[R_ITEMS * NWARPS];
@@ -2256,9 +2784,9 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
 
     constexpr uint64_t KMASK = 16 / sizeof(K) - 1, WMASK = 16 / sizeof(WS) - 1;
     auto tile_keys = [&](int buf, int d) {
-        return (K *)(dsm + buf * tile_bytes + (size_t)d * reorder_key_stride<D, KT>());
+        return (K *)(dsm + buf * tile_bytes + (size_t)d * small_reorder_key_stride<D, KT>());
     };
-    auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * reorder_key_stride<D, KT>()); };
+    auto tile_w = [&](int buf) { return (WS *)(dsm + buf * tile_bytes + (size_t)D * small_reorder_key_stride<D, KT>()); };
     // input index of the item at position e of the level (identity on level 0)
     auto orig = [&](uint64_t e) { return A.isrc ? (uint64_t)A.isrc[e] : e; };
     // carried indices of this thread's items of a tile (loaded one tile ahead)
@@ -2345,23 +2873,16 @@ __global__ void __launch_bounds__(BLOCK, sizeof(typename KT::T) == 4 ? 3 : 2) k_
         {
             CutBounds spb = {0.f, 0.f};
             if constexpr (KT::BAND) spb = band_bounds(sl.pivot);
-            auto left = [&](K k, uint64_t e) -> uint32_t {
-                if constexpr (KT::BAND) {
-                    if (sl.state == SEG_ALLLEFT) return 1u;
-                    const int sd = band_side(k, spb);
-                    if (sd != 0) return sd < 0 ? 1u : 0u;
-                    return KeyF64::lt(band_code_cold(&A.bs, A.isrc ? A.isrc[e] : e, A.coord), sl.pivot) ? 1u : 0u;
-                } else {
-                    return goes_left<KT>(k, sl) ? 1u : 0u;
-                }
+            auto side = [&](K k) -> int {
+                if constexpr (KT::BAND)
+                    return sl.state == SEG_ALLLEFT ? -1 : band_side(k, spb);
+                else
+                    return goes_left<KT>(k, sl) ? -1 : 1;
             };
-            // four loads in flight per thread
-            uint64_t e = la + threadIdx.x;
-            for (; e + 3 * BLOCK < le; e += 4 * BLOCK) {
-                const K k0 = kc[e], k1 = kc[e + BLOCK], k2 = kc[e + 2 * BLOCK], k3 = kc[e + 3 * BLOCK];
-                cnt += left(k0, e) + left(k1, e + BLOCK) + left(k2, e + 2 * BLOCK) + left(k3, e + 3 * BLOCK);
-            }
-            for (; e < le; e += BLOCK) cnt += left(kc[e], e);
+            auto exact = [&](uint64_t e) -> uint32_t {
+                return KeyF64::lt(band_code_cold(&A.bs, A.isrc ? A.isrc[e] : e, A.coord), sl.pivot) ? 1u : 0u;
+            };
+            cnt = count_left_keys<K>(kc, la, le, side, exact);
         }
         uint64_t agg;
         block_exscan_u64(cnt, sh, agg);

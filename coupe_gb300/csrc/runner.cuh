@@ -192,10 +192,18 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     const void *reorder_fn = carry ? (const void *)k_reorder<D, KT, WL, true> : (const void *)k_reorder<D, KT, WL, false>;
     CG_CK(cudaFuncSetAttribute(reorder_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)r_smem));
     const int g_reorder = occupancy_grid(reorder_fn, C.sms, BLOCK, r_smem);
+    // levels of small segments (below SMALL_SEG_ITEMS items on average) use
+    // the double-buffered k_reorder_small
+    const size_t rs_smem = small_reorder_smem<D, KT, WL>(carry);
+    const void *reorder_small_fn =
+        carry ? (const void *)k_reorder_small<D, KT, WL, true> : (const void *)k_reorder_small<D, KT, WL, false>;
+    CG_CK(cudaFuncSetAttribute(reorder_small_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs_smem));
+    const int g_reorder_small = occupancy_grid(reorder_small_fn, C.sms, BLOCK, rs_smem);
+    constexpr uint64_t SMALL_SEG_ITEMS = 4 * R_TILE;
     const uint64_t per_cta = (uint64_t)std::max(1, tu.reorder_chunks_per_cta);
-    // reorder chunks over the V items of a level's segments
-    auto chunk_of = [&](uint64_t V) {
-        uint64_t c = std::max<uint64_t>(R_TILE, (V + (uint64_t)g_reorder * per_cta - 1) / ((uint64_t)g_reorder * per_cta));
+    // reorder chunks over the V items of a level's segments, for a grid of g CTAs
+    auto chunk_of = [&](uint64_t V, int g) {
+        uint64_t c = std::max<uint64_t>(R_TILE, (V + (uint64_t)g * per_cta - 1) / ((uint64_t)g * per_cta));
         return (c + R_TILE - 1) / R_TILE * R_TILE;
     };
     const bool multi = R0.nsets > 1;
@@ -448,7 +456,9 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             st->levels = L + 1;
             return COUPE_ERR_OK;
         }
-        const uint64_t chunk = chunk_of(V);
+        const bool small_segs = tu.reorder_kernel == 0 ? V < S_max * SMALL_SEG_ITEMS : tu.reorder_kernel == 2;
+        const int g_r = small_segs ? g_reorder_small : g_reorder;
+        const uint64_t chunk = chunk_of(V, g_r);
         const uint64_t nchunks = (V + chunk - 1) / chunk;
         if (nchunks > R0.lbcap) {
             *err = "internal: more reorder chunks than look-back words";
@@ -480,8 +490,14 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
         R.S_ptr = S_dev;
         R.n_ptr = V_dev;
         const uint64_t rbytes = 2 * V * (D * sk + sw + si) - (ic ? 0 : V * si);
-        const unsigned r_grid = (unsigned)std::min<uint64_t>(g_reorder, nchunks);
-        if (carry) {
+        const unsigned r_grid = (unsigned)std::min<uint64_t>(g_r, nchunks);
+        if (small_segs) {
+            if (carry) {
+                CG_LAUNCH(KID_REORDER, rbytes, k_reorder_small<D, KT, WL, true><<<r_grid, BLOCK, rs_smem, s>>>(R));
+            } else {
+                CG_LAUNCH(KID_REORDER, rbytes, k_reorder_small<D, KT, WL, false><<<r_grid, BLOCK, rs_smem, s>>>(R));
+            }
+        } else if (carry) {
             CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, true><<<r_grid, BLOCK, r_smem, s>>>(R));
         } else {
             CG_LAUNCH(KID_REORDER, rbytes, k_reorder<D, KT, WL, false><<<r_grid, BLOCK, r_smem, s>>>(R));

@@ -133,7 +133,12 @@ def _main(argv=None):
     ap.add_argument("--side", type=int, default=512, help="hex mesh side (hexrib134M)")
     ap.add_argument("--sets", type=int, default=4096, help="sets (batched4096)")
     ap.add_argument("--total", type=int, default=200_000_000, help="about this many points (batched4096)")
+    ap.add_argument("--option", action="append", default=[], metavar="NAME=VALUE",
+                    help="a library option (coupe_gpu_set_option), e.g. reorder_kernel=2")
     a = ap.parse_args(argv)
+    for o in a.option:
+        name, value = o.split("=", 1)
+        coupe.set_option(name, int(value))
     dev = torch.device("cuda", 0)
     kw = {} if a.points is None else {"n": a.points}
     if a.workload == "batched4096":

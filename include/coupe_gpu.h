@@ -293,6 +293,9 @@ const char *coupe_gpu_kernel_name(int id);
  *                             every pass (by default the bins hold truncated
  *                             sums and a decision they cannot settle is
  *                             replayed from exact bins)
+ *   "reorder_kernel"          0 (default): per level, the bulk-copy reorder,
+ *                             or for segments below 8192 points on average
+ *                             the double-buffered one; 1 or 2 force either
  *   "autotune_cache"          1 (default): coupe_gpu_autotune returns the
  *                             schedule kept for a workload class tuned before
  *                             without timing again; 0: always time
