@@ -94,6 +94,21 @@ CG_HD uint32_t f64bits_to_f32bits(uint64_t b) {
     if (rem > half || (rem == half && (r & 1))) ++r;
     return sign | (uint32_t)r;  // r == 2^23 is the least normal, as encoded
 }
+// f32 -> f64 widening of a normal float or a zero in integer instructions
+// (exact: rebias the exponent, extend the fraction); false for subnormals,
+// infinities and NaN, which the caller widens with the f64 unit.
+CG_HD bool f32bits_to_f64bits(uint32_t u, uint64_t &out) {
+    const uint32_t e = (u >> 23) & 0xffu;
+    const uint64_t sgn = (uint64_t)(u & 0x80000000u) << 32;
+    if (e == 0) {
+        if (u & 0x7fffffu) return false;
+        out = sgn;
+        return true;
+    }
+    if (e == 255) return false;
+    out = sgn | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(u & 0x7fffffu) << 29);
+    return true;
+}
 
 CG_HD uint64_t f64_bits(double v) {
 #ifdef __CUDA_ARCH__
@@ -179,7 +194,16 @@ struct KeyF64 {
         if (e >= 255) return f32_from_bits(s | 0x7f800000u);
         return f32_from_bits(s | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
     }
-    CG_HD static T mid(T a, T b) { return from_f64((val(a) + val(b)) / 2.0); }
+    // (a + b) / 2 in f64: the sum by the f64 unit, the halving of a normal
+    // sum (exact) by decrementing its exponent field; zeros, subnormals,
+    // the smallest normals, infinities and NaN by the f64 division
+    CG_HD static T mid(T a, T b) {
+        const double s = val(a) + val(b);
+        const uint64_t sb = f64_bits(s);
+        const uint64_t ex = (sb >> 52) & 0x7ffu;
+        if (ex > 1 && ex < 0x7ffu) return enc_bits(sb - (1ull << 52));
+        return from_f64(s / 2.0);
+    }
     CG_HD static C cut_from_f64(double v) { return from_f64(v); }
     CG_HD static float approx_cut(C c) { return approx(c); }
     CG_HD static C cmid(C a, C b) { return mid(a, b); }
@@ -223,12 +247,24 @@ CG_HD float f32_step(float f, int dir) {  // the neighbouring float (ordered cod
 }
 CG_HD CutBounds band_bounds(uint64_t code) {
     const double c = KeyF64::val(code);
-    const float r = f32_from_bits(f64bits_to_f32bits(f64_bits(c)));  // RN32(c)
-    const double rd = (double)r;
+    const uint32_t rb = f64bits_to_f32bits(f64_bits(c));
+    const float r = f32_from_bits(rb);  // RN32(c)
+    // the sign of (double)r - c: from the ordered codes when r widens in
+    // integers and c is not NaN (codes order as the values do, -0 as +0),
+    // else by the f64 unit (NaN compares neither equal nor less)
+    int cmp;
+    uint64_t rdb;
+    if (code <= KeyF64::ORD_INF && f32bits_to_f64bits(rb, rdb)) {
+        const uint64_t rc = KeyF64::enc_bits(rdb);
+        cmp = rc == code ? 0 : (rc < code ? -1 : 1);
+    } else {
+        const double rd = (double)r;
+        cmp = rd == c ? 0 : (rd < c ? -1 : 1);
+    }
     CutBounds b;
-    if (rd == c) {
+    if (cmp == 0) {
         b.lo = b.hi = r;
-    } else if (rd < c) {
+    } else if (cmp < 0) {
         b.lo = r;
         b.hi = f32_step(r, 1);
     } else {
