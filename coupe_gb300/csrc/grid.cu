@@ -1,8 +1,12 @@
 // Rcb on a cartesian grid (coupe::Grid::rcb, coupe/src/cartesian/mod.rs:130-179,
 // cartesian/rcb.rs:52-281).  The split tree is built level by level:
-//   k_grid_axis_sums  for every subgrid of the level, the weight of each
-//                     slab across the split axis, one thread per slab,
-//                     summed in coupe's order (so f64 sums round alike);
+//   k_grid_slab_add   integer weights (order-free wrapping sums): one
+//                     coalesced pass over every cell, which finds its
+//                     subgrid by walking the tree built so far and adds its
+//                     weight to its slab (warp-aggregated atomics);
+//   k_grid_axis_sums  f64 weights: for every subgrid of the level, the weight
+//                     of each slab across the split axis, one thread per
+//                     slab, summed in coupe's order (so f64 sums round alike);
 //   host              the weighted median of those slab weights, replaying
 //                     rayon's fold_chunks with `threads` workers
 //                     (cartesian/rcb.rs:53-101), and the two halves;
@@ -72,26 +76,93 @@ __global__ void __launch_bounds__(BLOCK) k_grid_axis_sums(const W *__restrict__ 
         const GridSub g = subs[lo];
         const uint64_t p = g.off[g.coord] + (t - g.base);
         A acc = A(0);
-        if (D == 2) {
-            if (g.coord == 0) {
-                for (uint64_t y = g.off[1]; y < g.off[1] + g.size[1]; ++y) acc = GAcc<W>::add(acc, w[p + gw * y]);
-            } else {
-                for (uint64_t x = g.off[0]; x < g.off[0] + g.size[0]; ++x) acc = GAcc<W>::add(acc, w[x + gw * p]);
+        // one row of the slab, cnt cells `stride` apart, added in order; the
+        // loads of eight cells are issued before their adds
+        auto row = [&](uint64_t base, uint64_t stride, uint64_t cnt) {
+            uint64_t j = 0;
+            for (; j + 8 <= cnt; j += 8) {
+                W v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = w[base + (j + u) * stride];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) acc = GAcc<W>::add(acc, v[u]);
             }
+            for (; j < cnt; ++j) acc = GAcc<W>::add(acc, w[base + j * stride]);
+        };
+        if (D == 2) {
+            if (g.coord == 0)
+                row(p + gw * g.off[1], gw, g.size[1]);  // y
+            else
+                row(g.off[0] + gw * p, 1, g.size[0]);  // x
         } else if (g.coord == 0) {  // y outer, z inner
-            for (uint64_t y = g.off[1]; y < g.off[1] + g.size[1]; ++y)
-                for (uint64_t z = g.off[2]; z < g.off[2] + g.size[2]; ++z)
-                    acc = GAcc<W>::add(acc, w[p + gw * (y + gh * z)]);
+            for (uint64_t y = g.off[1]; y < g.off[1] + g.size[1]; ++y) row(p + gw * (y + gh * g.off[2]), gw * gh, g.size[2]);
         } else if (g.coord == 1) {  // z outer, x inner
-            for (uint64_t z = g.off[2]; z < g.off[2] + g.size[2]; ++z)
-                for (uint64_t x = g.off[0]; x < g.off[0] + g.size[0]; ++x)
-                    acc = GAcc<W>::add(acc, w[x + gw * (p + gh * z)]);
+            for (uint64_t z = g.off[2]; z < g.off[2] + g.size[2]; ++z) row(g.off[0] + gw * (p + gh * z), 1, g.size[0]);
         } else {  // x outer, y inner
-            for (uint64_t x = g.off[0]; x < g.off[0] + g.size[0]; ++x)
-                for (uint64_t y = g.off[1]; y < g.off[1] + g.size[1]; ++y)
-                    acc = GAcc<W>::add(acc, w[x + gw * (y + gh * p)]);
+            for (uint64_t x = g.off[0]; x < g.off[0] + g.size[0]; ++x) row(x + gw * (g.off[1] + gh * p), gw, g.size[1]);
         }
         out[t] = acc;
+    }
+}
+
+// Integer weights: the weight of every slab of the level's subgrids in one
+// pass over the cells in memory order.  A cell walks the split tree from the
+// root (first split on axis 1, then cycling) to its leaf; sub[leaf] is its
+// subgrid at this level (-1: a finished one) and the slot is the subgrid's
+// base plus the cell's position along the split axis.  The sums wrap like
+// coupe's release build and do not depend on the order of the adds.  Along
+// axis 1 or 2 a warp's 32 consecutive cells usually share one slot: then one
+// lane adds their sum.
+__device__ __forceinline__ void atomic_add_wrap(uint32_t *p, uint32_t v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add_wrap(uint64_t *p, uint64_t v) {
+    atomicAdd((unsigned long long *)p, (unsigned long long)v);
+}
+
+template <class W, int D>
+__global__ void __launch_bounds__(BLOCK) k_grid_slab_add(const W *__restrict__ w, uint64_t gw, uint64_t gh, uint64_t n,
+                                                         const int64_t *__restrict__ pos,
+                                                         const uint32_t *__restrict__ child,
+                                                         const int32_t *__restrict__ sub,
+                                                         const GridSub *__restrict__ subs,
+                                                         typename GAcc<W>::A *__restrict__ out) {
+    typedef typename GAcc<W>::A A;
+    const uint64_t stride = (uint64_t)gridDim.x * BLOCK;
+    // every lane of a warp runs the same number of iterations (the warp sums below)
+    const uint64_t iters = (n + stride - 1) / stride;
+    uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+    for (uint64_t it = 0; it < iters; ++it, i += stride) {
+        uint64_t slot = ~0ull;
+        A v = A(0);
+        if (i < n) {
+            uint64_t c[3];
+            c[0] = i % gw;
+            c[1] = D == 2 ? i / gw : (i / gw) % gh;
+            c[2] = D == 3 ? i / gw / gh : 0;
+            uint32_t node = 0;
+            int coord = 1;
+            int64_t at = pos[0];
+            while (at >= 0) {
+                node = child[node] + (c[coord] >= (uint64_t)at ? 1u : 0u);
+                at = pos[node];
+                coord = coord + 1 == D ? 0 : coord + 1;
+            }
+            const int32_t k = sub[node];
+            if (k >= 0) {
+                const GridSub &g = subs[k];
+                slot = g.base + (c[g.coord] - g.off[g.coord]);
+                v = (A)w[i];
+            }
+        }
+        const uint64_t s0 = __shfl_sync(0xffffffffu, slot, 0);
+        if (__all_sync(0xffffffffu, slot == s0)) {
+            // one slot for the warp: its sum, added once
+            A t = v;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if ((threadIdx.x & 31) == 0 && s0 != ~0ull) atomic_add_wrap(&out[s0], t);
+        } else if (slot != ~0ull) {
+            atomic_add_wrap(&out[slot], v);
+        }
     }
 }
 
@@ -317,8 +388,13 @@ int grid_run(DevCtx &C, const uint64_t *size, const W *d_w, uint64_t iters, uint
             if (err) *err = "too many splits";
             return COUPE_ERR_ALLOC;
         }
+        // workspace: the level's subgrids, its slab sums and (integer
+        // weights) the tree so far with each leaf's subgrid
         const size_t tab = subs.size() * sizeof(GridSub), tab_al = (tab + 255) & ~(size_t)255;
-        if ((rc = ensure_workspace(C, tab_al + slots * sizeof(A) + 256, err)) != COUPE_ERR_OK) return rc;
+        const size_t nb = tpos.size(), o_pos = tab_al + ((slots * sizeof(A) + 255) & ~(size_t)255),
+                     o_child = o_pos + ((nb * 8 + 255) & ~(size_t)255),
+                     o_sub = o_child + ((nb * 4 + 255) & ~(size_t)255), need = (F ? o_pos : o_sub + nb * 4) + 256;
+        if ((rc = ensure_workspace(C, need, err)) != COUPE_ERR_OK) return rc;
         GridSub *d_subs = (GridSub *)C.ws;
         A *d_sums = (A *)((char *)C.ws + tab_al);
         sums.resize(slots);
@@ -326,10 +402,34 @@ int grid_run(DevCtx &C, const uint64_t *size, const W *d_w, uint64_t iters, uint
                                                                                 (uint64_t)C.sms * 8));
         if ((e = cudaMemcpyAsync(d_subs, subs.data(), tab, cudaMemcpyHostToDevice, s)) != cudaSuccess)
             return cuda_fail(e, "grid table", err);
-        C.prof.begin(KID_GRID, n * sizeof(W), s);
-        k_grid_axis_sums<W, D><<<ga, BLOCK, 0, s>>>(d_w, gw, gh, d_subs, (uint32_t)subs.size(), slots, d_sums);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_grid_axis_sums", err);
-        C.prof.end(s);
+        if constexpr (F) {
+            C.prof.begin(KID_GRID, n * sizeof(W), s);
+            k_grid_axis_sums<W, D><<<ga, BLOCK, 0, s>>>(d_w, gw, gh, d_subs, (uint32_t)subs.size(), slots, d_sums);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_grid_axis_sums", err);
+            C.prof.end(s);
+        } else {
+            // the tree so far and each leaf's subgrid of this level
+            std::vector<int32_t> tsub(tpos.size(), -1);
+            {
+                size_t kk = 0;
+                for (const GNode &g : level)
+                    if (!(g.size[g.coord] == 0 || g.iters == 0)) tsub[g.index] = (int32_t)kk++;
+            }
+            int64_t *d_tpos = (int64_t *)((char *)C.ws + o_pos);
+            uint32_t *d_tchild = (uint32_t *)((char *)C.ws + o_child);
+            int32_t *d_tsub = (int32_t *)((char *)C.ws + o_sub);
+            if ((e = cudaMemcpyAsync(d_tpos, tpos.data(), nb * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(d_tchild, tchild.data(), nb * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(d_tsub, tsub.data(), nb * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+                (e = cudaMemsetAsync(d_sums, 0, slots * sizeof(A), s)) != cudaSuccess)
+                return cuda_fail(e, "grid level", err);
+            C.prof.begin(KID_GRID, n * sizeof(W), s);
+            k_grid_slab_add<W, D><<<gs, BLOCK, 0, s>>>(d_w, gw, gh, n, d_tpos, d_tchild, d_tsub, d_subs, d_sums);
+            if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "k_grid_slab_add", err);
+            C.prof.end(s);
+            // the host vectors above are read by the copies before they return
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "grid level", err);
+        }
         if ((e = cudaMemcpyAsync(sums.data(), d_sums, slots * sizeof(A), cudaMemcpyDeviceToHost, s)) !=
                 cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess)
