@@ -71,7 +71,8 @@ class Stats(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("max_nbk", ctypes.c_int), ("hist_ctas_per_sm", ctypes.c_int),
-                ("reorder_chunks_per_cta", ctypes.c_int), ("device_ms", ctypes.c_double)]
+                ("reorder_chunks_per_cta", ctypes.c_int), ("hist_waves", ctypes.c_int),
+                ("device_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {n: getattr(self, n) for n, _ in self._fields_}

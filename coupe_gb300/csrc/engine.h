@@ -48,6 +48,7 @@ struct Tuning {
     int max_nbk = 10;                // bisection steps per histogram pass (2^max_nbk bins)
     int reorder_chunks_per_cta = 1;  // reorder chunks per resident CTA
     int hist_ctas_per_sm = 0;        // histogram CTAs per SM (0: as many as fit)
+    int hist_waves = 1;              // histogram grid: this many waves of resident CTAs
     int exact_f64_hist = 0;          // 1: f64 weights always binned exactly
     int reorder_kernel = 0;          // 0: by segment size; 1: k_reorder (bulk copies); 2: k_reorder_small
     // Failure handling (not scheduling): polls of a reorder chunk's bounded

@@ -924,6 +924,7 @@ static int *option_slot(const char *name) {
     if (!std::strcmp(name, "max_nbk")) return &t.max_nbk;
     if (!std::strcmp(name, "reorder_chunks_per_cta")) return &t.reorder_chunks_per_cta;
     if (!std::strcmp(name, "hist_ctas_per_sm")) return &t.hist_ctas_per_sm;
+    if (!std::strcmp(name, "hist_waves")) return &t.hist_waves;
     if (!std::strcmp(name, "exact_f64_hist")) return &t.exact_f64_hist;
     if (!std::strcmp(name, "reorder_kernel")) return &t.reorder_kernel;
     if (!std::strcmp(name, "lookback_spin_limit")) return &t.lookback_spin_limit;
@@ -955,7 +956,7 @@ namespace {
 // COUPE_GPU_TUNE_CACHE names a file, in that file (one line per class,
 // appended when a class is first tuned, read at the first lookup).
 struct TuneEntry {
-    int max_nbk, hist_ctas_per_sm, reorder_chunks_per_cta;
+    int max_nbk, hist_ctas_per_sm, reorder_chunks_per_cta, hist_waves;
     double ms;
 };
 std::mutex g_tune_mu;
@@ -987,8 +988,8 @@ void tune_load_locked() {
     if (!f) return;
     char key[128];
     TuneEntry e;
-    while (std::fscanf(f, "%127s %d %d %d %lf", key, &e.max_nbk, &e.hist_ctas_per_sm, &e.reorder_chunks_per_cta,
-                       &e.ms) == 5)
+    while (std::fscanf(f, "%127s %d %d %d %d %lf", key, &e.max_nbk, &e.hist_ctas_per_sm, &e.reorder_chunks_per_cta,
+                       &e.hist_waves, &e.ms) == 6)
         g_tune[key] = e;
     std::fclose(f);
 }
@@ -999,7 +1000,8 @@ void tune_store_locked(const std::string &key, const TuneEntry &e) {
     if (!path || !*path) return;
     FILE *f = std::fopen(path, "a");
     if (!f) return;
-    std::fprintf(f, "%s %d %d %d %.6f\n", key.c_str(), e.max_nbk, e.hist_ctas_per_sm, e.reorder_chunks_per_cta, e.ms);
+    std::fprintf(f, "%s %d %d %d %d %.6f\n", key.c_str(), e.max_nbk, e.hist_ctas_per_sm, e.reorder_chunks_per_cta,
+                 e.hist_waves, e.ms);
     std::fclose(f);
 }
 
@@ -1012,8 +1014,8 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
                                   const void *d_weights, const uint32_t *iter_counts, double tolerance, int mode,
                                   void *stream, int repeats, struct coupe_gpu_tuning *best) {
     // Candidate schedules: bisection steps per histogram pass, histogram CTAs
-    // per SM and reorder chunks per CTA.  None changes the ids, so the
-    // fastest (median device time of `repeats` runs) is kept process-wide.
+    // per SM and waves of them, and reorder chunks per CTA.  None changes the
+    // ids, so the fastest (median device time of `repeats` runs) is kept.
     cg::Tuning &t = cg::tuning();
     const cg::Tuning keep = t;
     const int reps = repeats < 1 ? 1 : (repeats > 15 ? 15 : repeats);
@@ -1030,10 +1032,12 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
             t.max_nbk = hit->second.max_nbk;
             t.hist_ctas_per_sm = hit->second.hist_ctas_per_sm;
             t.reorder_chunks_per_cta = hit->second.reorder_chunks_per_cta;
+            t.hist_waves = hit->second.hist_waves;
             if (best) {
                 best->max_nbk = t.max_nbk;
                 best->hist_ctas_per_sm = t.hist_ctas_per_sm;
                 best->reorder_chunks_per_cta = t.reorder_chunks_per_cta;
+                best->hist_waves = t.hist_waves;
                 best->device_ms = hit->second.ms;
             }
             return COUPE_ERR_OK;
@@ -1043,11 +1047,13 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
     cg::Tuning best_t = keep;
     for (int nbk : {10, 9, 8, 7, 6})
         for (int hc : {0, 3, 2})
-            for (int rc : {1, 2}) {
+            for (int rc : {1, 2})
+                for (int hw : {1, 2}) {
                 t = keep;
                 t.max_nbk = nbk;
                 t.hist_ctas_per_sm = hc;
                 t.reorder_chunks_per_cta = rc;
+                t.hist_waves = hw;
                 std::vector<double> ms;
                 for (int r = 0; r < reps + 1; ++r) {
                     const coupe_err rc_ = coupe_gpu_rcb_batched(d_partition, nsets, set_offsets, dimension, d_points,
@@ -1070,12 +1076,13 @@ enum coupe_err coupe_gpu_autotune(uint64_t *d_partition, uint64_t nsets, const u
     if (cg::tuning().autotune_cache) {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         tune_store_locked(key, TuneEntry{best_t.max_nbk, best_t.hist_ctas_per_sm, best_t.reorder_chunks_per_cta,
-                                         best_ms});
+                                         best_t.hist_waves, best_ms});
     }
     if (best) {
         best->max_nbk = best_t.max_nbk;
         best->hist_ctas_per_sm = best_t.hist_ctas_per_sm;
         best->reorder_chunks_per_cta = best_t.reorder_chunks_per_cta;
+        best->hist_waves = best_t.hist_waves;
         best->device_ms = best_ms;
     }
     return COUPE_ERR_OK;

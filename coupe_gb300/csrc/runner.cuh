@@ -213,6 +213,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     const int approx = tu.exact_f64_hist ? 0 : 1;
     int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
     if (tu.hist_ctas_per_sm > 0) g_hist = std::min(g_hist, tu.hist_ctas_per_sm * C.sms);
+    g_hist *= std::max(1, std::min(tu.hist_waves, 16));
     if (multi) {
         CG_LAUNCH(KID_ROOT, 0,
                   k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,

@@ -289,6 +289,8 @@ const char *coupe_gpu_kernel_name(int id);
  *   "max_nbk"                 bisection steps per histogram pass (1..10)
  *   "reorder_chunks_per_cta"  work chunks per resident CTA in the reorder
  *   "hist_ctas_per_sm"        histogram CTAs per SM (0: as many as fit)
+ *   "hist_waves"              histogram grid in this many waves of resident
+ *                             CTAs (1..16; default 1)
  *   "exact_f64_hist"          1: bin f64 weights as exact fixed-point sums in
  *                             every pass (by default the bins hold truncated
  *                             sums and a decision they cannot settle is
@@ -323,6 +325,7 @@ struct coupe_gpu_tuning {
 	int max_nbk;
 	int hist_ctas_per_sm;
 	int reorder_chunks_per_cta;
+	int hist_waves;   /* histogram grid: waves of resident CTAs */
 	double device_ms; /* median device time of the chosen schedule */
 };
 
@@ -331,9 +334,10 @@ struct coupe_gpu_tuning {
  * candidate schedule of the knobs above, `repeats` timed runs each after one
  * warm-up, and keeps the fastest process-wide (the ids are the same under
  * every schedule).  `best` (may be NULL) receives the choice; d_partition
- * holds the ids of the last run.  30 candidates (bisection steps per pass
- * 6-10, histogram CTAs per SM 0/3/2, reorder chunks per CTA 1/2): budget
- * about 30 * (repeats + 1) runs of the workload.  The choice is kept per
+ * holds the ids of the last run.  60 candidates (bisection steps per pass
+ * 6-10, histogram CTAs per SM 0/3/2, reorder chunks per CTA 1/2, one or two
+ * waves of histogram CTAs): budget about 60 * (repeats + 1) runs of the
+ * workload.  The choice is kept per
  * workload class (points and sets rounded down to powers of two, dimension,
  * weight type, mode, deepest iteration count): a later call for the same
  * class applies the kept schedule at once, runs nothing and leaves

@@ -140,7 +140,7 @@ def test_autotune_keeps_ids(coupe, oracle_mod):
     iters = rng.integers(1, 9, len(sizes))
     pts, w, off, it = _sets(rng, sizes, 3, "i64", iters)
     want = oracle_mod.rcb_sets(pts, w, off, it, 0.01, mode=1, threads=0)
-    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta")
+    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta", "hist_waves")
     keep = {k: coupe.get_option(k) for k in names + ("autotune_cache",)}
     try:
         coupe.set_option("autotune_cache", 0)  # time the candidates here
@@ -149,7 +149,7 @@ def test_autotune_keeps_ids(coupe, oracle_mod):
         ids = torch.zeros(len(pts), dtype=torch.int64, device="cuda")
         best = coupe.autotune_device(ids, dp, dw, off, it, 0.01, mode="f32key_f64band", repeats=1)
         assert best["max_nbk"] in (6, 7, 8, 9, 10) and best["hist_ctas_per_sm"] in (0, 2, 3)
-        assert best["reorder_chunks_per_cta"] in (1, 2) and best["device_ms"] > 0
+        assert best["reorder_chunks_per_cta"] in (1, 2) and best["hist_waves"] in (1, 2) and best["device_ms"] > 0
         assert {k: coupe.get_option(k) for k in names} == {k: best[k] for k in names}
         assert np.array_equal(ids.cpu().numpy().astype(np.uint64), want)
         assert np.array_equal(_gpu(coupe, torch, pts, w, off, it, 0.01, "f32key_f64band"), want)
@@ -168,7 +168,7 @@ def test_autotune_keeps_its_choice_per_workload_class(coupe, tmp_path, monkeypat
     sizes = [int(x) for x in rng.integers(5_000, 50_000, 9)]
     iters = np.full(len(sizes), 7)
     pts, w, off, it = _sets(rng, sizes, 2, "i32", iters)
-    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta")
+    names = ("max_nbk", "hist_ctas_per_sm", "reorder_chunks_per_cta", "hist_waves")
     keep = {k: coupe.get_option(k) for k in names + ("autotune_cache",)}
     try:
         coupe.set_option("autotune_cache", 1)

@@ -291,7 +291,7 @@ def test_rib_end_to_end(coupe, oracle_mod):
                                    {"force_index_path": 1, "reorder_chunks_per_cta": 7},
                                    {"hist_ctas_per_sm": 1}, {"hist_ctas_per_sm": 2, "max_nbk": 9},
                                    {"sync_levels": 1}, {"sync_levels": 1, "max_nbk": 2}, {"max_nbk": 2},
-                                   {"reorder_kernel": 1}, {"reorder_kernel": 2},
+                                   {"reorder_kernel": 1}, {"reorder_kernel": 2}, {"hist_waves": 3},
                                    {"reorder_kernel": 1, "force_index_path": 1}, {"reorder_kernel": 2, "force_index_path": 1}])
 def test_scheduling_knobs_do_not_change_ids(coupe, oracle_mod, knobs):
     """Part ids through the index path, fewer bisection steps per pass and
