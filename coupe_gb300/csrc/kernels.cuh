@@ -1789,8 +1789,66 @@ __device__ __forceinline__ void scan_list_block(const Seg<KT> *__restrict__ segs
 // ---------------------------------------------------------------------------
 // k_decide: replays coupe's split loop (recursive_bisection.rs:470-572) for
 // up to nbk steps per segment from its bins.  One warp per listed segment;
-// every lane computes the same decisions.
+// every lane computes the same decisions.  The FP64 pipe bounds a decision
+// step on this GPU, so the two f64 tests of a step are first settled in f32
+// or integer arithmetic with a proven error bound (ImbalanceTest, band_far);
+// only values within that bound of the threshold take the f64 expressions.
 // ---------------------------------------------------------------------------
+
+// coupe's imbalance test |(w - ideal) / ideal| <= tol, evaluated in f64
+// (recursive_bisection.rs:547-551).  With f32 values wf = RN32(w),
+// idf = RN32(ideal) (normal) and rinv = RN32(1 / |idf|), the f32 quotient
+// q = RN32(|RN32(wf - idf)| rinv) lies within 2^-22 ((|w| + |ideal|) /
+// |ideal| + q) of |w - ideal| / |ideal| (three roundings of 2^-24 on each
+// term, the conversions of w and ideal included), and coupe's f64 quotient
+// within 2^-51 of the same; so e = 2^-21 ((|wf| + |idf|) rinv + q) bounds
+// their distance with room for the rounding of e and of q +- e.  q + e at or
+// below RD32(tol) proves the test true, q - e above RU32(tol) proves it
+// false; anything else (and every non-finite or extreme case) takes the
+// f64 division.
+struct ImbalanceTest {
+    double ideal, tol;
+    float idf, rinv, tlo, thi;
+    bool fast;
+};
+__device__ __forceinline__ ImbalanceTest imbalance_test(double ideal, double tol) {
+    ImbalanceTest t;
+    t.ideal = ideal;
+    t.tol = tol;
+    t.idf = (float)ideal;
+    const float a = fabsf(t.idf);
+    t.rinv = 1.0f / a;
+    t.tlo = __double2float_rd(tol);
+    t.thi = __double2float_ru(tol);
+    t.fast = a >= 0x1p-100f && a <= 0x1p100f;  // false for NaN
+    return t;
+}
+template <class WT>
+__device__ __forceinline__ bool imbalance_within(const ImbalanceTest &t, typename WT::V w) {
+    if (t.fast) {
+        const float wf = (float)w;
+        const float q = fabsf(wf - t.idf) * t.rinv;
+        const float e = 0x1p-21f * ((fabsf(wf) + fabsf(t.idf)) * t.rinv + q);
+        const float up = q + e, dn = q - e;
+        if (up <= t.tlo && up <= 0x1p127f) return true;  // (inf and NaN fail)
+        if (dn > t.thi) return false;
+    }
+    return fabs((WT::f64(w) - t.ideal) / t.ideal) <= t.tol;
+}
+
+// Band form: true when hi <= t + d certainly fails for every distance d the
+// f64 step could compute from the smallest right key k (its items' x lie in
+// [t, max(next32(k), RU32(t))] =: [t, M]).  t + RN(x - t) rounds to at most
+// M + 2^-51 A with A = max(|M|, |RD32(t)|) >= |x|, |t|, so RD32(hi) above
+// RU32(M + 2^-50 A) proves hi > t + d.  Integer and f32 instructions only.
+__device__ __forceinline__ bool band_far(float k, uint64_t t, uint64_t hi) {
+    const CutBounds tb = band_bounds(t), hb = band_bounds(hi);
+    const float nk = f32_step(k, 1);
+    const float M = fmaxf(nk, tb.hi);
+    const float A = fmaxf(fabsf(M), fabsf(tb.lo));
+    if (!isfinite(k) || !isfinite(nk) || !isfinite(tb.lo) || !isfinite(M) || !isfinite(A)) return false;
+    return hb.lo > __fadd_ru(M, __fmul_ru(A, 0x1p-50f));
+}
 template <class KT, class WT>
 __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__restrict__ list, const uint32_t k,
                                            Hist<KT, WT> H, int nbk, double tol, uint32_t *flags, RunScalars *rs,
@@ -1924,6 +1982,8 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
         else if (sg.sumx == SUMX_RIGHT)
             sum = WT::sub(sum, WT::value(segs[s - 1].xq, fs));
     }
+    const double ideal = WT::f64(sum) / 2.0;
+    const ImbalanceTest imt = imbalance_test(ideal, tol);
     K lo = sg.lo, hi = sg.hi;
     uint64_t prev = sg.prev;
     int lo_b = 0, hi_b = NB;
@@ -1994,9 +2054,13 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
         // distance of the nearest item on the right (recursive_bisection.rs:487):
         // exact, or in the band form bounds [dl, dh] of it
         typename KT::A dl, dh;
+        bool far = false;  // band form: hi <= t + d is certainly false (band_far)
         if constexpr (KT::BAND) {
             if (kminO == NONE) {
                 dl = dh = KT::inf();
+            } else if (band_far(KT::unord(kminO), t, hi)) {
+                far = true;
+                dl = dh = 0.0;  // finite; the near tests below are false
             } else {
                 double xl, xh;
                 band_interval(KT::unord(kminO), xl, xh);
@@ -2045,17 +2109,16 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
                 wl_hi = fixed_to_f64(ql + (unsigned __int128)count * ((((unsigned __int128)1) << qb) - 1), fs);
             }
         }
-        const double ideal = WT::f64(sum) / 2.0;
         // recursive_bisection.rs:547-563.  imbalance <= tol holds on an
         // interval of weight_left values that contains sum/2 (f64 rounding is
         // monotone), so two ends that agree settle it, unless both fail on
         // either side of sum/2; `hi <= t + dist` is monotone in dist.
-        // (f64 division is slow here: the upper end only with truncated bins)
-        const bool p_lo = fabs((WT::f64(wl) - ideal) / ideal) <= tol;
-        const bool p_hi = apx ? fabs((WT::f64(wl_hi) - ideal) / ideal) <= tol : p_lo;
+        // (the upper end only with truncated bins)
+        const bool p_lo = imbalance_within<WT>(imt, wl);
+        const bool p_hi = apx ? imbalance_within<WT>(imt, wl_hi) : p_lo;
         const bool spans = apx && ideal != 0.0 && WT::f64(wl) <= ideal && ideal <= WT::f64(wl_hi);
         const bool imb_yes = p_lo && p_hi, imb_no = !p_lo && !p_hi && !(spans && tol >= 0.0);
-        const bool near_lo = hv <= tv + dl, near_hi = hv <= tv + dh;
+        const bool near_lo = !far && hv <= tv + dl, near_hi = !far && hv <= tv + dh;
         const bool stop = count == prev || near_lo || imb_yes;
         bool need_x = false, need_w = false;
         if (!stop) {
@@ -2164,7 +2227,7 @@ __device__ __forceinline__ void decide_one(Seg<KT> *segs, const uint32_t *__rest
     }
 }
 
-// One warp per listed segment (decide_one); then the last CTA to finish lists
+// One warp per listed segment (decide_one), spc segments per CTA; then the last CTA to finish lists
 // the segments still searching and the prefix of their sizes for the next
 // pass (list2, P2, rs->nactive).
 template <class KT, class WT>
@@ -2173,14 +2236,16 @@ __global__ void __launch_bounds__(BLOCK) k_decide(Seg<KT> *segs, const uint32_t 
                                                   RunScalars *rs, const uint64_t *nlist_ptr,
                                                   const int32_t *__restrict__ set_fs,
                                                   const int32_t *__restrict__ set_qb, uint32_t *list2, uint64_t *P2,
-                                                  ChildArgs<KT> ca) {
+                                                  ChildArgs<KT> ca, uint32_t spc) {
     __shared__ uint32_t s_last;
     if (cta_halted(rs)) return;
     // the list's length from the device (the grid is an upper bound); every
     // CTA reads it before the last one's scan overwrites it
     if (nlist_ptr) nlist = (uint32_t)*nlist_ptr;
-    const uint32_t k = blockIdx.x * NWARPS + (threadIdx.x >> 5);
-    if (k < nlist) decide_one<KT, WT>(segs, list, k, H, nbk, tol, flags, rs, set_fs, set_qb);
+    // spc of the CTA's warps take a segment each (fewer than all when the
+    // list is short: the segments' FP64 work then spreads over more SMs)
+    const uint32_t w = threadIdx.x >> 5, k = blockIdx.x * spc + w;
+    if (w < spc && k < nlist) decide_one<KT, WT>(segs, list, k, H, nbk, tol, flags, rs, set_fs, set_qb);
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) s_last = atomicAdd(&rs->decide_done, 1u) == gridDim.x - 1;

@@ -150,6 +150,15 @@ static inline int occupancy_grid(const void *fn, int sms, int block, size_t smem
     return per * sms;
 }
 
+// Segments per k_decide CTA (one warp each): as few as keep the grid within
+// the `resident` CTAs of one wave, so that short lists spread their
+// decisions, whose FP64 work bounds them, over the SMs (256 segments: 256
+// CTAs of one working warp rather than 32 CTAs of eight).
+static inline uint32_t decide_segs_per_cta(uint64_t S, int resident) {
+    const uint64_t r = (uint64_t)std::max(1, resident);
+    return (uint32_t)std::min<uint64_t>(NWARPS, std::max<uint64_t>(1, (S + r - 1) / r));
+}
+
 // What the set-up of a run hands to its level loop.
 struct RunSetup {
     uint64_t n = 0, iters = 0, lbcap = 0, bytes = 0;
@@ -214,6 +223,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
     int g_hist = occupancy_grid((const void *)k_hist<KT, WL>, C.sms, BLOCK, 0);
     if (tu.hist_ctas_per_sm > 0) g_hist = std::min(g_hist, tu.hist_ctas_per_sm * C.sms);
     g_hist *= std::max(1, std::min(tu.hist_waves, 16));
+    const int g_decide = occupancy_grid((const void *)k_decide<KT, WL>, C.sms, BLOCK, 0);
     if (multi) {
         CG_LAUNCH(KID_ROOT, 0,
                   k_roots<KT, WL><<<(R0.nroots + 255) / 256, 256, 0, s>>>(B.segs[0], B.list[0], B.P[0], B.roots,
@@ -302,7 +312,8 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             }
             return (int)COUPE_ERR_OK;
         };
-        const unsigned decide_grid = (unsigned)((S_max + NWARPS - 1) / NWARPS);
+        const uint32_t decide_spc = decide_segs_per_cta(S_max, g_decide);
+        const unsigned decide_grid = (unsigned)((S_max + decide_spc - 1) / decide_spc);
         ChildArgs<KT> no_ch;
         std::memset(&no_ch, 0, sizeof(no_ch));
         const uint64_t decide_bytes = S_max * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord));
@@ -338,7 +349,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
             CG_LAUNCH(KID_DECIDE, decide_bytes,
                       k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[0], 0u, H, nbk, a.tolerance,
                                                                      B.flags, B.rs, S_dev, set_fs, set_qb, B.list[1],
-                                                                     B.P[1], no_ch));
+                                                                     B.P[1], no_ch, decide_spc));
             // Speculative passes over the list the last scan left: their
             // kernels read its count and return at once when no segment is
             // searching.  The lists alternate; the last pass's decide builds
@@ -357,7 +368,7 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                           k_decide<KT, WL><<<decide_grid, BLOCK, 0, s>>>(segs, B.list[li], 0u, H, nbk, a.tolerance,
                                                                          B.flags, B.rs, &B.rs->nactive, set_fs, set_qb,
                                                                          B.list[li ^ 1], B.P[li ^ 1],
-                                                                         final_pass ? ch : no_ch));
+                                                                         final_pass ? ch : no_ch, decide_spc));
                 li ^= 1;
             }
             active_list[L] = li;
@@ -391,10 +402,11 @@ int run_levels(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *er
                                                                   H, nbk, n, B.rs, nullptr, hsrc, bs, coord, segs,
                                                                   set_fs, set_qb));
                 ++st->hist_passes;
+                const uint32_t spc = decide_segs_per_cta(nlist, g_decide);
                 CG_LAUNCH(KID_DECIDE, nlist * NB * (4 + 8 * WL::LIMBS + sizeof(typename KT::Ord)),
-                          k_decide<KT, WL><<<(unsigned)((nlist + NWARPS - 1) / NWARPS), BLOCK, 0, s>>>(
+                          k_decide<KT, WL><<<(unsigned)((nlist + spc - 1) / spc), BLOCK, 0, s>>>(
                               segs, B.list[li], (uint32_t)nlist, H, nbk, a.tolerance, B.flags, B.rs, nullptr, set_fs,
-                              set_qb, B.list[li ^ 1], B.P[li ^ 1], no_ch));
+                              set_qb, B.list[li ^ 1], B.P[li ^ 1], no_ch, spc));
                 li ^= 1;
                 CG_CK(cudaMemcpyAsync(h_rs, B.rs, sizeof(RunScalars), cudaMemcpyDeviceToHost, s));
                 CG_CK(cudaStreamSynchronize(s));
