@@ -378,6 +378,21 @@ CG_HD double fixed_to_f64(unsigned __int128 Qbits, int s) {
         }
         x = sh;
     }
+    // |value| = m 2^(x - s) with m < 2^53: a normal result is assembled
+    // from its fields (no FP64 instruction), the rest by ldexp
+    const int hm = 63 - (hb <= 52 ? clz128((unsigned __int128)m) - 64 : 11);  // top bit of m
+    const int e = x - s + hm;                                                    // unbiased exponent
+    if (e >= -1022 && e <= 1023) {
+        const uint64_t mn = m << (52 - hm);  // in [2^52, 2^53), exact
+        const uint64_t b = ((uint64_t)(e + 1023) << 52) | (mn & 0x000fffffffffffffull) | (neg ? 1ull << 63 : 0);
+#ifdef __CUDA_ARCH__
+        return __longlong_as_double((long long)b);
+#else
+        double r;
+        memcpy(&r, &b, 8);
+        return r;
+#endif
+    }
     double r = ldexp((double)m, x - s);
     return neg ? -r : r;
 }

@@ -762,31 +762,63 @@ __device__ __forceinline__ void build_sorted_cuts(typename KT::C lo, typename KT
     }
 }
 
+// Grid position of a key in the interval [lo, hi] of nb bins:
+// f = (approx(k) - l) sc + s with l = approx_cut(lo), sc = nb / RN32(hi - lo)
+// (within 2^-23 of nb / (hi - lo): two f32 roundings) and the shift
+// s = RN32(l - lo) sc, which corrects for l != lo (f64 interval ends; it is
+// below the margin's ulp term, so its own rounding is negligible); i.e.
+// (approx(k) - lo) nb / (hi - lo) up to roundings.  No f64 division.
+struct GridMap {
+    float l, sc, s;
+    bool ok;  // finite, non-empty interval of normal f32 width
+};
+template <class KT>
+__device__ __forceinline__ GridMap grid_map(typename KT::C lo, typename KT::C hi, int nb) {
+    GridMap g;
+    g.l = KT::approx_cut(lo);
+    float w;
+    if constexpr (sizeof(typename KT::C) == 4) {
+        w = hi - lo;  // f32 interval ends: l == lo
+        g.s = 0.0f;
+        g.sc = (float)nb / w;
+    } else {
+        const double lod = KT::cval(lo), hid = KT::cval(hi);
+        w = (float)(hid - lod);
+        g.sc = (float)nb / w;
+        g.s = (float)((double)g.l - lod) * g.sc;
+    }
+    g.ok = w >= 1.17549435e-38f && isfinite(g.l) && isfinite(g.sc) && isfinite(g.s);  // false for NaN
+    return g;
+}
+
 // Bin lookup: an arithmetic first guess (cuts are close to an even grid),
-// corrected against the exact sorted cuts; a binary search when the
-// interval is degenerate or not finite.
+// corrected against the exact sorted cuts (the guess, or its neighbour when
+// it is one bin off); a binary search when the interval is degenerate or not
+// finite, or the guess is further off.
 struct BinGuess {
-    float lo, scale;
+    float lo, scale, shift;
     int fast;
 };
 
-template <class KT>
-__device__ __forceinline__ BinGuess bin_guess(typename KT::C lo, typename KT::C hi, int nb) {
+__device__ __forceinline__ BinGuess bin_guess(const GridMap &m) {
     BinGuess g;
-    const float l = KT::approx_cut(lo), h = KT::approx_cut(hi);
-    const float sc = (float)nb / (h - l);
-    g.lo = l;
-    g.scale = sc;
-    g.fast = (h > l) && isfinite(l) && isfinite(h) && isfinite(sc);
+    g.lo = m.l;
+    g.scale = m.sc;
+    g.shift = m.s;
+    g.fast = m.ok;
     return g;
 }
 
 template <class KT>
 __device__ __forceinline__ int bin_sorted(typename KT::T key, const typename KT::T *cuts, int nb, const BinGuess &g) {
     if (g.fast) {
-        float f = (KT::approx(key) - g.lo) * g.scale;
+        float f = fmaf(KT::approx(key) - g.lo, g.scale, g.shift);
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
-        const int b = __float2int_rz(f);
+        int b = __float2int_rz(f);
+        if (b > 0 && KT::lt(key, cuts[b - 1]))
+            --b;
+        else if (b < nb - 1 && !KT::lt(key, cuts[b]))
+            ++b;
         // the guess, if its two cuts confirm it; else the binary search
         // (cuts crowded at the precision of the keys make the guess far off)
         if ((b == 0 || !KT::lt(key, cuts[b - 1])) && (b == nb - 1 || KT::lt(key, cuts[b]))) return b;
@@ -811,10 +843,18 @@ __device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const flo
     int b = -1;
     float4 q;
     if (g.fast) {
-        float f = (k - g.lo) * g.scale;
+        float f = fmaf(k - g.lo, g.scale, g.shift);
         f = fminf(fmaxf(f, 0.0f), (float)(nb - 1));
         b = __float2int_rz(f);
         q = cbb[b];
+        // one step to the neighbour when the guess is one bin off
+        if (b > 0 && !(k > q.x)) {
+            --b;
+            q = cbb[b];
+        } else if (b < nb - 1 && k > q.y) {
+            ++b;
+            q = cbb[b];
+        }
         // the guess stands if the bounds of its two cuts confirm it
         if (!((b == 0 || k > q.x) && (b == nb - 1 || !(k > q.y)))) b = -1;
     }
@@ -850,43 +890,43 @@ __device__ __forceinline__ int bin_band_exact(int b, uint64_t c, const uint64_t 
 }
 
 // ---------------------------------------------------------------------------
-// Bins without looking at the cuts.  With l, h the floats near the interval
-// ends and sc = nb / (h - l), a key k in [lo, hi] has the grid position
-// f = (approx(k) - l) * sc.  Every cut c_r lies within `dev` of the even grid
-// point l + (r+1)(h-l)/nb:
-//   KeyF32: each of the nbk f32 midpoints (a + b) / 2 of cuts within
-//           [lo, hi] adds at most half an ulp of M = max(|l|, |h|);
-//   KeyF64: f64 midpoints are exact to far below an f32 ulp, but l and h
-//           are truncated to f32 (one ulp of M) and so is approx(k);
-//   KeyBand: as KeyF64, plus one ulp for a cut's f32 band [RD32(c), RU32(c)].
-// f itself is (approx(k) - l) nb / (h - l) to 4 roundings of 2^-24, i.e. at
-// most (nb + 1) 2^-22 away for keys inside the interval (a subtraction with
-// a subnormal result is exact).  So when the fraction of f is more than
-// m = 2 (sc dev + (nb + 1) 2^-22) away from both bin edges (twice the bound),
-// floor(f) is the key's bin and, in the band form, the key is outside every
-// cut's band; the other keys take the exact search.  Intervals where m would
-// exceed 1/4 (narrow intervals far from zero, or ranges near the limits of
-// f32) use the exact search for every key (m = 2 never passes the test).
+// Bins without looking at the cuts.  A key's grid position
+// f = (approx(k) - l) sc + s (grid_map) is (approx(k) - lo) nb / (hi - lo) to
+// within E = (nb + 1) 2^-21 for keys inside the interval (the roundings of
+// approx(k) - l and of the fused multiply-add, 2^-24 each, and sc's 2^-23, of
+// values below nb + 1, with room to spare).  Every cut c_r lies within `dev` of its grid
+// point lo + (r+1)(hi - lo)/nb, and the key within `dk` of the value whose
+// bin is wanted (ulps of M = max(|lo|, |hi|)):
+//   KeyF32: dev = nbk/2 (each of the at most nbk f32 midpoints on a cut's
+//           path adds at most half an ulp), dk = 0;
+//   KeyF64: f64 midpoints are exact to far below an f32 ulp (dev ~ 0), and
+//           approx(k) truncates the key to f32: dk = 1;
+//   KeyBand: dev ~ 0; a key in a cut's band [RD32(c), RU32(c)] lies within
+//           one ulp of the cut, and x within half an ulp of its key: 1.
+// So when the fraction of f is more than m = 1.01 sc (dev + dk) ulp + E
+// (+ 2^-20 for the rounding of m) away from both bin edges, floor(f) is the
+// key's bin and, in the band form, the key is outside every cut's band; the
+// other keys take the exact search.  Intervals where m would exceed 1/4
+// (narrow intervals far from zero, or ranges near the limits of f32) use the
+// exact search for every key (m = 2 never passes the test).
 // ---------------------------------------------------------------------------
 struct FastBin {
-    float l, sc, m, m1;  // m1 = 1 - m
+    float l, sc, s, m, m1;  // m1 = 1 - m
 };
 template <class KT>
-__device__ __forceinline__ FastBin fast_bin(typename KT::C lo, typename KT::C hi, int nbk) {
+__device__ __forceinline__ FastBin fast_bin(const GridMap &g, typename KT::C hi, int nbk) {
     FastBin r;
-    const float l = KT::approx_cut(lo), h = KT::approx_cut(hi);
     const float nb = (float)(1 << nbk);
-    const float sc = nb / (h - l);
-    r.l = l;
-    r.sc = sc;
+    r.l = g.l;
+    r.sc = g.sc;
+    r.s = g.s;
     r.m = 2.0f;
     r.m1 = -1.0f;
-    const float M = fmaxf(fabsf(l), fabsf(h));
-    if (!(h > l) || !isfinite(sc) || !(M > 1e-30f) || !(M < 1e37f)) return r;
-    // error of the cuts (and of approx(k)) in ulps of M
-    const float ulps = KT::BAND ? 4.0f : (sizeof(typename KT::T) == 8 ? 4.0f : (float)nbk);
+    const float M = fmaxf(fabsf(g.l), fabsf(KT::approx_cut(hi)));
+    if (!g.ok || !(M > 1e-30f) || !(M < 1e37f)) return r;
+    const float ulps = (!KT::BAND && sizeof(typename KT::T) == 4) ? 0.5f * (float)nbk : 1.0f;
     const float u = M * 1.1920929e-7f + 1.4012985e-45f;  // >= ulp(M)
-    const float m = 2.0f * (sc * 1.01f * ulps * u + (nb + 1.0f) * 2.3841858e-7f);
+    const float m = 1.01f * ulps * u * g.sc + (nb + 1.0f) * 4.7683716e-7f + 9.5367432e-7f;
     if (m < 0.25f) {
         r.m = m;
         r.m1 = 1.0f - m;
@@ -1047,7 +1087,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
             for (int l = 0; l < L; ++l) wsw[i * L + l] = 0;
         }
         __syncwarp();
-        const BinGuess g = bin_guess<KT>(lo, hi, NB);
+        const BinGuess g = bin_guess(grid_map<KT>(lo, hi, NB));
         uint64_t xacc[L];
 #pragma unroll
         for (int l = 0; l < L; ++l) xacc[l] = 0;
@@ -1226,8 +1266,9 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
             for (int l = 0; l < L; ++l) sw[i * L + l] = 0;
         }
         __syncthreads();
-        const BinGuess g = bin_guess<KT>(lo, hi, NB);
-        const FastBin fb = fast_bin<KT>(lo, hi, nbk);
+        const GridMap gm = grid_map<KT>(lo, hi, NB);
+        const BinGuess g = bin_guess(gm);
+        const FastBin fb = fast_bin<KT>(gm, hi, nbk);
         const EdgeTest<KT> et = edge_test<KT>(lo, hi);
         bool xpend = false;  // band form: a decision waits for an exact minimum
         uint32_t xkey = 0;
@@ -1344,7 +1385,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                     }
                     const bool binned = valid && !nan;
                     const bool below = et.below(kv[i]), above = !below && et.above(kv[i]);
-                    const float f = (KT::approx(kv[i]) - fb.l) * fb.sc;
+                    const float f = fmaf(KT::approx(kv[i]) - fb.l, fb.sc, fb.s);
                     const int bg = __float2int_rz(f);
                     const float fr = f - (float)bg;
                     const bool fast = (uint32_t)bg < (uint32_t)NB && fr > fb.m && fr < fb.m1;
@@ -1368,7 +1409,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                             else if (b0 < NB - 1 && !KT::lt(kv[i], cuts[b0]))
                                 bin = b0 + 1;
                         } else {
-                            bin = bin_sorted<KT>(kv[i], cuts, NB, BinGuess{0.f, 0.f, 0});
+                            bin = bin_sorted<KT>(kv[i], cuts, NB, BinGuess{0.f, 0.f, 0.f, 0});
                         }
                     }
                     if (PD) sl = sl || (binned && KT::ord(kv[i]) == xkey);
