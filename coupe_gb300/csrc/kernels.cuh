@@ -878,6 +878,11 @@ __device__ __forceinline__ int bin_band(float k, const uint64_t *cuts, const flo
 // The bin from cut b on, from the f64 code: the first cut above c, by binary
 // search (a narrow interval can hold hundreds of cuts within one f32 band).
 __device__ __forceinline__ int bin_band_exact(int b, uint64_t c, const uint64_t *cuts, int nb) {
+    // usually cut b or b + 1 is the first above c (the key lies in one
+    // cut's band); crowded cuts take the binary search
+    if (b >= nb - 1 || KeyF64::lt(c, cuts[b])) return b;
+    if (b + 1 >= nb - 1 || KeyF64::lt(c, cuts[b + 1])) return b + 1;
+    b += 2;
     int r = nb - 1;  // answer in [b, r]
     while (b < r) {
         const int m = (b + r) >> 1;
@@ -1485,16 +1490,23 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                 // single call site keeps the search's registers out of the
                 // loop above)
                 const bool fin = base + (uint64_t)BLOCK * HI >= b;
-                if (__any_sync(0xffffffffu, slow != 0) || (fin && qn)) {
+                // the item slots in which some lane marked an item (usually
+                // one or two); then a last round that flushes the rest
+                const uint32_t anyb = KT::BAND || PD ? __reduce_or_sync(0xffffffffu, slow) : 0u;
+                if (anyb != 0 || (fin && qn)) {
+                    uint32_t mm = anyb;
 #pragma unroll 1
-                    for (int i = 0; i <= HI; ++i) {
-                        const bool bit = i < HI && ((slow >> i) & 1u);
+                    for (;;) {
+                        const bool last = mm == 0;
+                        const int i = last ? HI : __ffs(mm) - 1;
+                        mm &= mm - 1;
+                        const bool bit = !last && ((slow >> i) & 1u);
                         const uint32_t m = __ballot_sync(0xffffffffu, bit);
                         if (bit)
                             s_q[warp][qn + __popc(m & ((1u << lane) - 1))] =
                                 (uint32_t)(base - a) + i * BLOCK + threadIdx.x;
                         qn += __popc(m);
-                        if (qn >= 32 || (i == HI && fin && qn)) {
+                        if (qn >= 32 || (last && fin && qn)) {
                             const uint32_t cnt = qn < 32 ? qn : 32u;
                             __syncwarp();
                             if (lane < cnt) slow_item(a + s_q[warp][lane]);
@@ -1505,6 +1517,7 @@ __global__ void __launch_bounds__(BLOCK, WT::LIMBS > 1 ? 3 : HIST_MINB) k_hist(c
                             if (lane < qn) s_q[warp][lane] = v;
                         }
                         __syncwarp();
+                        if (last) break;
                     }
                 }
             }
