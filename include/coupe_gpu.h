@@ -253,8 +253,9 @@ enum coupe_err coupe_gpu_imbalance_device(uint64_t num_parts, const uint64_t *d_
  *
  * The first call on each device (with that device current) does a one-time
  * set-up: it looks up the scratch's device address with
- * cudaGetSymbolAddress and sets the kernels' shared-memory limit.  Make that
- * first call before any stream capture.  The set-up is kept for the life of
+ * cudaGetSymbolAddress and sets the kernels' shared-memory limit.  Every call
+ * reads its result back and synchronises its stream, so no call can be made
+ * while the stream is being captured.  The set-up is kept for the life of
  * the process: after cudaDeviceReset on a device, this entry point must not
  * be called on that device again.  A launch error left pending by the
  * caller's own earlier work is reported as such (COUPE_ERR_CRASH) before any
