@@ -615,4 +615,62 @@ struct RunScalars {
 // needed more passes than were queued (the host finishes the run).
 __host__ __device__ __forceinline__ bool run_halted(const RunScalars *rs) { return (rs->err | rs->stall) != 0; }
 
+// ---------------------------------------------------------------------------
+// f32 pairs: a value as hi + lo (|lo| <= ulp(hi)/2), with error-free sums
+// and fused-multiply-add products (Dekker 1971, Shewchuk 1997); about 44
+// significant bits at f32 speed.  GB300's FP64 pipe runs at 1/64 of the f32
+// rate, so per-point f64 arithmetic is replaced by these where the result
+// needs only a bounded error (or a bound decides it exactly).  They rely on
+// f32 operations rounding to nearest one at a time (no contraction: the
+// library is built with -fmad=false).
+// ---------------------------------------------------------------------------
+struct F2 {
+    float h, l;
+};
+__device__ __forceinline__ F2 f2_two_sum(float a, float b) {
+    const float s = a + b, v = s - a;
+    return {s, (a - (s - v)) + (b - v)};
+}
+__device__ __forceinline__ F2 f2_fast(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ F2 f2_sub(F2 a, F2 b) {
+    const F2 s = f2_two_sum(a.h, -b.h);
+    return f2_fast(s.h, s.l + (a.l - b.l));
+}
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return f2_fast(p, e);
+}
+__device__ __forceinline__ void f2_add(F2 &acc, F2 x) {
+    const F2 s = f2_two_sum(acc.h, x.h);
+    acc = f2_fast(s.h, s.l + (acc.l + x.l));
+}
+// x as an f32 pair; false when |x| lies outside [2^-50, 2^50] (zeros pass)
+__device__ __forceinline__ bool f2_split(double x, F2 &r) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if ((b << 1) == 0) {
+        r = {0.0f, 0.0f};
+        return true;
+    }
+    if (e < 1023 - 50 || e > 1023 + 50) return false;
+    const uint64_t M = (b & 0x000fffffffffffffull) | (1ull << 52);  // |x| = M 2^(e - 1075)
+    const uint64_t H = (M + 0x0fffffffull + ((M >> 29) & 1)) >> 29;  // RN(M / 2^29), at most 2^24
+    const int32_t R = (int32_t)((int64_t)M - (int64_t)(H << 29));    // |R| <= 2^28
+    const float sh = __uint_as_float((uint32_t)(e - 1046 + 127) << 23);  // 2^(e - 1046)
+    const float sl = __uint_as_float((uint32_t)(e - 1075 + 127) << 23);  // 2^(e - 1075)
+    float h = (float)(uint32_t)H * sh, l = (float)R * sl;  // exact scalings; (float)R rounds to nearest
+    if (b >> 63) {
+        h = -h;
+        l = -l;
+    }
+    r = {h, l};
+    return true;
+}
+
 }  // namespace cg

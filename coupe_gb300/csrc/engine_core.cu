@@ -233,6 +233,85 @@ __global__ void __launch_bounds__(BLOCK) k_moments(const double *__restrict__ pt
     }
 }
 
+// ---------------------------------------------------------------------------
+// The unweighted sums (coupe's matrix) without f64 arithmetic per point:
+// each coordinate is split into an f32 pair (hi = RN32(x), lo = RN32(x - hi),
+// hi + lo within 2^-48 |x|) by integer instructions, and the offsets, their
+// products and the per-thread sums are pair arithmetic (error-free sums and
+// fused-multiply-add products; Dekker 1971, Shewchuk 1997), good to about
+// 2^-44 relative.  GB300's FP64 pipe runs at 1/64 of the f32 rate, and the f64
+// version of this pass was bound by it.  A point with a coordinate outside
+// [2^-50, 2^50] in magnitude (zeros excepted) is added in f64 instead.  The
+// per-thread sums then join the same fixed-order f64 reduction.  (F2 and
+// its helpers are in common.cuh.)
+// ---------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(BLOCK) k_moments_f2(const double *__restrict__ pts, uint64_t n, double *partial) {
+    constexpr int K = moment_terms<D>();
+    __shared__ double sh[K][NWARPS];
+    F2 acc[K];
+    double slow[K];  // points outside the pairs' range
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        acc[k] = {0.0f, 0.0f};
+        slow[k] = 0.0;
+    }
+    double sft[D];
+    F2 sft2[D];
+    bool sft_ok = true;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        sft[d] = pts[d];
+        sft_ok = f2_split(sft[d], sft2[d]) && sft_ok;
+    }
+    for (uint64_t i = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (uint64_t)gridDim.x * BLOCK) {
+        double p[D];
+        F2 o[D];
+        bool ok = sft_ok;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            p[d] = pts[i * D + d];
+            F2 q;
+            ok = f2_split(p[d], q) && ok;
+            o[d] = f2_sub(q, sft2[d]);
+        }
+        if (ok) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) f2_add(acc[1 + d], o[d]);
+            int k = 1 + D;
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b2 = a; b2 < D; ++b2, ++k) f2_add(acc[k], f2_mul(o[a], o[b2]));
+        } else {
+            double od[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                od[d] = __dsub_rn(p[d], sft[d]);
+                slow[1 + d] = __dadd_rn(slow[1 + d], od[d]);
+            }
+            int k = 1 + D;
+#pragma unroll
+            for (int a = 0; a < D; ++a)
+#pragma unroll
+                for (int b2 = a; b2 < D; ++b2, ++k) slow[k] = __dadd_rn(slow[k], __dmul_rn(od[a], od[b2]));
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double v = __dadd_rn(__dadd_rn((double)acc[k].h, (double)acc[k].l), slow[k]);
+        for (int off = 16; off > 0; off >>= 1) v = __dadd_rn(v, __shfl_down_sync(0xffffffffu, v, off));
+        if (lane == 0) sh[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+        double v = 0.0;
+        for (int w2 = 0; w2 < NWARPS; ++w2) v = __dadd_rn(v, sh[threadIdx.x][w2]);
+        partial[blockIdx.x * K + threadIdx.x] = v;
+    }
+}
+
 // Symmetric eigenvectors by cyclic Jacobi rotations (Golub & Van Loan,
 // Matrix Computations, section 8.5), columns of v.
 static void sym_eigen(const double *a_in, int n, double *ev, double *v) {
@@ -352,8 +431,12 @@ int rib_matrix(DevCtx &C, uint64_t n, int dim, const double *d_points, cudaStrea
     std::unique_ptr<double[]> h(new double[RIB_GRID * K]);
     const bool weighted = d_weights != nullptr;
     if (!weighted) {
-        rc = dim == 2 ? launch_moments<2, double>(d_points, n, nullptr, d_part, s, err)
-                      : launch_moments<3, double>(d_points, n, nullptr, d_part, s, err);
+        if (dim == 2)
+            k_moments_f2<2><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_part);
+        else
+            k_moments_f2<3><<<RIB_GRID, BLOCK, 0, s>>>(d_points, n, d_part);
+        const cudaError_t le = cudaGetLastError();
+        rc = le == cudaSuccess ? (int)COUPE_ERR_OK : cuda_fail(le, "k_moments_f2", err);
     } else if (wtype == COUPE_INT) {
         rc = dim == 2 ? launch_moments<2>(d_points, n, (const int32_t *)d_weights, d_part, s, err)
                       : launch_moments<3>(d_points, n, (const int32_t *)d_weights, d_part, s, err);
