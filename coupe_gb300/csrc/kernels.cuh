@@ -372,6 +372,27 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
         mx[d] = ord_f64(-1.7976931348623157e308);
     }
     K *outs[3] = {k0, k1, k2};
+    // The basis change with f32 keys (one point set): f32-pair arithmetic
+    // decides most points (point_f2), given the matrix entries as pairs.  The
+    // lanes of a warp share one exact box (merged whenever a lane computed
+    // an exact value), so that inputs in a drifting order, such as a mesh
+    // in index order, still leave most points inside it; mnf / mxf bound
+    // that box from outside (mnf >= its minimum, mxf <= its maximum).
+    float mnf[3], mxf[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        mnf[d] = INFINITY;
+        mxf[d] = -INFINITY;
+    }
+    F2 m2[D * D];
+    bool mfast = false;
+    if constexpr (sizeof(K) == 4) {
+        if (M.on && sets.count <= 1) {
+            mfast = true;
+#pragma unroll
+            for (int i = 0; i < D * D; ++i) mfast = f2_split(M.m[i], m2[i]) && mfast;
+        }
+    }
     // Several sets: each CTA converts one contiguous range of tiles and each
     // thread sends its box to the set table whenever its items enter another
     // set (a few times per thread).
@@ -385,6 +406,8 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             atomicMax((unsigned long long *)&sets.bmax[cur.s * 3 + d], (unsigned long long)mx[d]);
             mn[d] = ord_f64(1.7976931348623157e308);
             mx[d] = ord_f64(-1.7976931348623157e308);
+            mnf[d] = INFINITY;
+            mxf[d] = -INFINITY;
         }
     };
     // q receives the raw bits of the (mapped) coordinates; without a basis
@@ -410,6 +433,92 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                 mx[d] = o > mx[d] ? o : mx[d];
             }
     };
+    // One point of a basis change with f32 keys, without f64 instructions:
+    // y_r = coupe's chain ((m_r0 p0 + m_r1 p1) + m_r2 p2) in f64 is estimated
+    // by an f32 pair Y_r within e_r = 2^-39 sum_c |m_rc p_c| (the pair products
+    // and sums are good to about 2^-44 of that sum, the chain's own roundings
+    // to 5 2^-53 of it, and the f32 sum of the magnitudes to 2^-22).  The
+    // key RN32(y_r) is Y_r's high part when [Y_r - e_r, Y_r + e_r] holds no
+    // f32 rounding boundary, and the point cannot move the box when its
+    // bounds lie strictly inside (mnf, mxf).  false: take the f64 chain.
+    auto point_f2 = [&](const double *p, K *kk) -> bool {
+        F2 pp[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c)
+            if (!f2_split(p[c], pp[c])) return false;
+        F2 y[D];
+        float e[D];
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            F2 acc = f2_mul(m2[r * D], pp[0]);
+            float sabs = fabsf(m2[r * D].h * pp[0].h);
+#pragma unroll
+            for (int c = 1; c < D; ++c) {
+                f2_add(acc, f2_mul(m2[r * D + c], pp[c]));
+                sabs += fabsf(m2[r * D + c].h * pp[c].h);
+            }
+            y[r] = acc;
+            e[r] = sabs * 0x1p-39f;
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            const uint32_t hb = __float_as_uint(y[r].h);
+            const uint32_t ex = (hb >> 23) & 0xffu;
+            if (ex < 25u || ex > 253u) return false;  // zero, tiny or near the f32 range's end
+            const float u = __uint_as_float((ex - 23u) << 23);              // ulp(|Y_r.h|)
+            const float up = 0.5f * u;                                       // half the gap away from zero
+            const float down = (hb & 0x7fffffu) ? 0.5f * u : 0.25f * u;     // half the gap towards zero
+            const float away = (hb >> 31) ? -y[r].l : y[r].l;               // Y_r - Y_r.h, away from zero
+            if (!(away + e[r] < up && e[r] - away < down)) return false;
+            kk[r] = y[r].h;
+        }
+#pragma unroll
+        for (int r = 0; r < D; ++r) {
+            const float slack = fabsf(y[r].l) + e[r] + fabsf(y[r].h) * 0x1p-22f;
+            if (!(y[r].h - slack > mnf[r]) || !(y[r].h + slack < mxf[r])) return false;
+        }
+        return true;
+    };
+    // after the f64 chain: f32 bounds of the thread's exact box
+    auto shadow = [&]() {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const uint64_t a = mn[d], b = mx[d];
+            const uint64_t qa = (a & 0x8000000000000000ull) ? (a & 0x7fffffffffffffffull) : ~a;
+            const uint64_t qb = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
+            const float fa = f32_from_bits(f64bits_to_f32bits(qa)), fb = f32_from_bits(f64bits_to_f32bits(qb));
+            mnf[d] = isfinite(fa) ? f32_step(fa, 1) : INFINITY;     // >= the minimum
+            mxf[d] = isfinite(fb) ? f32_step(fb, -1) : -INFINITY;   // <= the maximum
+        }
+    };
+    if (mfast && n > 0) {
+        // Seed the box with one exact point per thread, drawn across the
+        // whole input (an odd-multiplier hash of the thread's index), and
+        // merged over the block: its extremes start near the input's, so few
+        // points need the f64 chain for the box later.  Seeds are input
+        // points, so the box stays exact.
+        const uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
+        uint64_t q[D];
+        point(pts + ((g * 0x9E3779B97F4A7C15ull) % n) * D, q);
+        const int sl = threadIdx.x & 31, sw = threadIdx.x >> 5;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const uint64_t a = warp_min_u64(mn[d]), b = warp_max_u64(mx[d]);
+            if (sl == 0) {
+                red[2 * d][sw] = a;
+                red[2 * d + 1][sw] = b;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            for (int w2 = 0; w2 < NWARPS; ++w2) {
+                mn[d] = red[2 * d][w2] < mn[d] ? red[2 * d][w2] : mn[d];
+                mx[d] = red[2 * d + 1][w2] > mx[d] ? red[2 * d + 1][w2] : mx[d];
+            }
+        __syncthreads();  // red is written again at the end
+        shadow();
+    }
     // Tiles of CONV_TILE points move to shared memory by asynchronous copies
     // (the next tile lands while this one is converted): consecutive threads
     // copy consecutive 16-byte pieces of the AoS input, so the loads are
@@ -454,15 +563,39 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
 #pragma unroll
         for (int r = 0; r < CONV_TILE / BLOCK; ++r) {
             const uint32_t j = r * BLOCK + threadIdx.x;
+            bool exact = false;  // this lane evaluated the f64 chain
             if (j < np) {
                 if (multi && (p0 + j < cur.beg || p0 + j >= cur.end)) {
                     flush();
                     cur.move(sets, p0 + j);
                 }
-                uint64_t q[D];
-                point(&tile[buf][j * D], q);
+                bool done = false;
+                if constexpr (sizeof(K) == 4) {
+                    if (mfast) {
+                        K kk[D];
+                        if (point_f2(&tile[buf][j * D], kk)) {
 #pragma unroll
-                for (int d = 0; d < D; ++d) outs[d][p0 + j] = KT::from_f64_bits(q[d]);
+                            for (int d = 0; d < D; ++d) outs[d][p0 + j] = kk[d];
+                            done = true;
+                        }
+                    }
+                }
+                if (!done) {
+                    uint64_t q[D];
+                    point(&tile[buf][j * D], q);
+#pragma unroll
+                    for (int d = 0; d < D; ++d) outs[d][p0 + j] = KT::from_f64_bits(q[d]);
+                    exact = true;
+                }
+            }
+            if (mfast && __any_sync(0xffffffffu, exact)) {
+                // the warp's box from its lanes' exact values
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    mn[d] = warp_min_u64(mn[d]);
+                    mx[d] = warp_max_u64(mx[d]);
+                }
+                shadow();
             }
         }
         __syncthreads();  // the buffer is free for the tile after next

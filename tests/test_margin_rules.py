@@ -9,7 +9,10 @@
   * imbalance_test / imbalance_within (k_decide): coupe's f64 test
     |(w - ideal) / ideal| <= tol (recursive_bisection.rs:547-551), settled
     from f32 arithmetic when the estimate is clear of tol;
-  * band_far (k_decide, band form): hi <= t + dist certainly false.
+  * band_far (k_decide, band form): hi <= t + dist certainly false;
+  * f2_split and the f32-pair Rib key and box shortcuts (point_f2 in
+    k_convert): the key RN32 of coupe's f64 basis-change chain, and the box
+    of the mapped points, as the f64 chain gives them.
 
 Each replay asserts that whenever a shortcut decides, it decides as the
 exact expression does.  The GPU parity tests check the kernels end to end.
@@ -202,3 +205,133 @@ def test_band_far_shortcut():
                 far_count += 1
                 assert not (hi <= t + dl) and not (hi <= t + dh), (k, t, hi)
     assert far_count > 5_000
+
+
+# ---------------------------------------------------------------- f32 pairs
+def _f2_split(x):
+    """f2_split (common.cuh): hi = RN32(x), lo = RN32(x - hi), from the f64
+    fields with integer operations."""
+    import struct
+    b = struct.unpack("<Q", struct.pack("<d", x))[0]
+    e = (b >> 52) & 0x7FF
+    if (b << 1) & 0xFFFFFFFFFFFFFFFF == 0:
+        return F32(0), F32(0)
+    if not 1023 - 50 <= e <= 1023 + 50:
+        return None  # the kernels take the f64 path
+    M = (b & ((1 << 52) - 1)) | (1 << 52)
+    H = (M + 0x0FFFFFFF + ((M >> 29) & 1)) >> 29
+    R = M - (H << 29)
+    sh = np.frombuffer(struct.pack("<I", (e - 1046 + 127) << 23), dtype=F32)[0]
+    sl = np.frombuffer(struct.pack("<I", (e - 1075 + 127) << 23), dtype=F32)[0]
+    h, l = F32(F32(H) * sh), F32(F32(R) * sl)
+    return (-h, -l) if b >> 63 else (h, l)
+
+
+def test_f2_split_matches_rounding():
+    rng = np.random.default_rng(3)
+    for it in range(20_000):
+        x = float(rng.standard_normal() * 2.0 ** rng.integers(-49, 49))
+        if it % 7 == 0:
+            x = float(F32(x)) * (1 + 2.0 ** -24)  # halfway cases
+        r = _f2_split(x)
+        if r is not None:
+            assert r[0] == F32(x) and r[1] == F32(x - float(F32(x)))
+
+
+def _pair_ops():
+    def two_sum(a, b):
+        s = F32(a + b)
+        v = F32(s - a)
+        return s, F32((a - (s - v)) + (b - v))
+
+    def fast(a, b):
+        s = F32(a + b)
+        return s, F32(b - (s - a))
+
+    def fma(a, b, c):
+        return F32(np.float64(a) * np.float64(b) + np.float64(c))
+
+    def mul(a, b):
+        p = F32(a[0] * b[0])
+        e = fma(a[0], b[0], -p)
+        e = fma(a[0], b[1], e)
+        e = fma(a[1], b[0], e)
+        return fast(p, e)
+
+    def add(acc, x):
+        s = two_sum(acc[0], x[0])
+        return fast(s[0], F32(s[1] + F32(acc[1] + x[1])))
+    return mul, add
+
+
+def test_rib_key_shortcut():
+    """point_f2 (k_convert): the key RN32 of coupe's f64 chain
+    ((m0 p0 + m1 p1) + m2 p2) is the pair estimate's high part whenever no
+    f32 rounding boundary lies within the bound of it."""
+    mul, add = _pair_ops()
+    rng = np.random.default_rng(5)
+    fast_n = 0
+    for trial in range(12):
+        D = 3 if trial % 2 == 0 else 2
+        Q, _ = np.linalg.qr(rng.standard_normal((D, D)))
+        sc = 10.0 ** rng.uniform(-3, 5)
+        for _ in range(400):
+            p = rng.standard_normal(D) * sc * np.array([1, 10, 100][:D])
+            if trial % 3 == 0:
+                p = np.round(p, 2)
+            pp = [_f2_split(float(v)) for v in p]
+            if any(v is None for v in pp):
+                continue
+            for r in range(D):
+                y = Q[r, 0] * p[0]
+                for c in range(1, D):
+                    y = y + Q[r, c] * p[c]
+                m = [_f2_split(float(v)) for v in Q[r]]
+                if any(v is None for v in m):
+                    continue
+                acc = mul(m[0], pp[0])
+                sabs = F32(abs(F32(m[0][0] * pp[0][0])))
+                for c in range(1, D):
+                    acc = add(acc, mul(m[c], pp[c]))
+                    sabs = F32(sabs + abs(F32(m[c][0] * pp[c][0])))
+                e = F32(sabs * F32(2.0 ** -39))
+                hb = int(np.asarray(acc[0], dtype=F32).view(np.uint32))
+                ex = (hb >> 23) & 0xFF
+                if not 25 <= ex <= 253:
+                    continue
+                u = np.frombuffer(np.uint32((ex - 23) << 23).tobytes(), dtype=F32)[0]
+                up = F32(0.5) * u
+                down = F32(0.5) * u if hb & 0x7FFFFF else F32(0.25) * u
+                away = -acc[1] if hb >> 31 else acc[1]
+                if F32(away + e) < up and F32(e - away) < down:
+                    fast_n += 1
+                    assert acc[0] == F32(y), (p, r)
+    assert fast_n > 5_000
+
+
+def test_rib_box_shortcut():
+    """point_f2's box test: a point is skipped only when its bounds lie
+    strictly inside the f32 bounds of the running exact box; the box found
+    equals the exact one, also for sorted and tied values."""
+    rng = np.random.default_rng(9)
+    for trial in range(12):
+        n = 3000
+        y = rng.standard_normal(n) * 10.0 ** rng.uniform(-3, 6)
+        if trial % 3 == 0:
+            y = np.sort(y)
+        if trial % 3 == 1:
+            y = np.round(y, 1)
+        e = np.abs(y) * 2.0 ** -40 * rng.uniform(0.5, 4, n)
+        est = y + rng.uniform(-1, 1, n) * e * 0.9
+        yh = est.astype(F32)
+        yl = (est - yh.astype(np.float64)).astype(F32)
+        ef = e.astype(F32)
+        mn, mx, mnf, mxf = np.inf, -np.inf, F32(np.inf), F32(-np.inf)
+        for i in range(n):
+            slack = F32(F32(abs(yl[i]) + ef[i]) + F32(abs(yh[i]) * F32(2.0 ** -22)))
+            if F32(yh[i] - slack) > mnf and F32(yh[i] + slack) < mxf:
+                continue
+            mn, mx = min(mn, y[i]), max(mx, y[i])
+            mnf = np.nextafter(F32(mn), F32(np.inf))
+            mxf = np.nextafter(F32(mx), F32(-np.inf))
+        assert mn == y.min() and mx == y.max()
