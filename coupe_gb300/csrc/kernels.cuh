@@ -356,9 +356,11 @@ __device__ __forceinline__ uint64_t band_code_lean(const BandSrc &bs, uint64_t o
 // f32`, recursive_bisection.rs:674-679), optionally after the Rib basis change
 // p' = M p accumulated column by column (geometry.rs:203-205), and the f64
 // bounding box (BoundingBox::from_points, geometry.rs:33-78: NaN never
-// updates, the fold starts at f64::MAX / f64::MIN), per point set.
+// updates, the fold starts at f64::MAX / f64::MIN), per point set.  F2K:
+// the instance for a basis change with f32 keys and one point set, which
+// evaluates it in f32 pairs (point_f2); the others keep their registers.
 // ---------------------------------------------------------------------------
-template <int D, class KT>
+template <int D, class KT, bool F2K = false>
 __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pts, uint64_t n, Mat M,
                                                    typename KT::T *__restrict__ k0,
                                                    typename KT::T *__restrict__ k1,
@@ -386,7 +388,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
     }
     F2 m2[D * D];
     bool mfast = false;
-    if constexpr (sizeof(K) == 4) {
+    if constexpr (F2K && sizeof(K) == 4) {
         if (M.on && sets.count <= 1) {
             mfast = true;
 #pragma unroll
@@ -491,7 +493,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             mxf[d] = isfinite(fb) ? f32_step(fb, -1) : -INFINITY;   // <= the maximum
         }
     };
-    if (mfast && n > 0) {
+    if (F2K && mfast && n > 0) {
         // Seed the box with one exact point per thread, drawn across the
         // whole input (an odd-multiplier hash of the thread's index), and
         // merged over the block: its extremes start near the input's, so few
@@ -570,7 +572,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                     cur.move(sets, p0 + j);
                 }
                 bool done = false;
-                if constexpr (sizeof(K) == 4) {
+                if constexpr (F2K && sizeof(K) == 4) {
                     if (mfast) {
                         K kk[D];
                         if (point_f2(&tile[buf][j * D], kk)) {
@@ -588,7 +590,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                     exact = true;
                 }
             }
-            if (mfast && __any_sync(0xffffffffu, exact)) {
+            if (F2K && mfast && __any_sync(0xffffffffu, exact)) {
                 // the warp's box from its lanes' exact values
 #pragma unroll
                 for (int d = 0; d < D; ++d) {

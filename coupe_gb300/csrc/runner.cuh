@@ -741,9 +741,15 @@ int run_typed(DevCtx &C, const RunArgs &a, coupe_gpu_stats *st, std::string *err
     M.on = a.has_matrix ? 1 : 0;
     for (int i = 0; i < 9; ++i) M.m[i] = a.matrix[i];
     const uint64_t sk = sizeof(K), sw = sizeof(typename WT::S);
-    CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
-              k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1], B.keys[0][2],
-                                                          B.rs, sets));
+    if (M.on && sizeof(K) == 4 && sets.count <= 1) {
+        CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
+                  k_convert<D, KT, true><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1],
+                                                                    B.keys[0][2], B.rs, sets));
+    } else {
+        CG_LAUNCH(KID_CONVERT, n * (D * 8 + D * sk),
+                  k_convert<D, KT><<<g_stream, BLOCK, 0, s>>>(a.d_points, n, M, B.keys[0][0], B.keys[0][1],
+                                                              B.keys[0][2], B.rs, sets));
+    }
     const typename WT::S *w_in = (const typename WT::S *)a.d_weights;
     if (a.weights_ready) CG_CK(cudaStreamWaitEvent(s, a.weights_ready, 0));
     if (WT::LIMBS > 1) {
