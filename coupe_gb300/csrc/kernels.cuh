@@ -375,17 +375,15 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
     }
     K *outs[3] = {k0, k1, k2};
     // The basis change with f32 keys (one point set): f32-pair arithmetic
-    // decides most points (point_f2), given the matrix entries as pairs.  The
-    // lanes of a warp share one exact box (merged whenever a lane computed
-    // an exact value), so that inputs in a drifting order, such as a mesh
-    // in index order, still leave most points inside it; mnf / mxf bound
-    // that box from outside (mnf >= its minimum, mxf <= its maximum).
-    float mnf[3], mxf[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        mnf[d] = INFINITY;
-        mxf[d] = -INFINITY;
-    }
+    // decides most points (point_f2), given the matrix entries as pairs.  A
+    // point whose f64 value was computed bounds the block's box: s_fmn holds
+    // the least f32 above such a value (as an ordered code), s_fmx the
+    // greatest below; a point strictly between them cannot be an extreme
+    // (those values are input points'), so its exact value is not needed.
+    // One box per block, seeded across the whole input, leaves few points to
+    // the f64 chain even for inputs in a drifting order (a mesh in index
+    // order).
+    __shared__ uint32_t s_fmn[3], s_fmx[3];
     F2 m2[D * D];
     bool mfast = false;
     if constexpr (F2K && sizeof(K) == 4) {
@@ -408,8 +406,6 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             atomicMax((unsigned long long *)&sets.bmax[cur.s * 3 + d], (unsigned long long)mx[d]);
             mn[d] = ord_f64(1.7976931348623157e308);
             mx[d] = ord_f64(-1.7976931348623157e308);
-            mnf[d] = INFINITY;
-            mxf[d] = -INFINITY;
         }
     };
     // q receives the raw bits of the (mapped) coordinates; without a basis
@@ -477,49 +473,37 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
 #pragma unroll
         for (int r = 0; r < D; ++r) {
             const float slack = fabsf(y[r].l) + e[r] + fabsf(y[r].h) * 0x1p-22f;
-            if (!(y[r].h - slack > mnf[r]) || !(y[r].h + slack < mxf[r])) return false;
+            const float mnf = unord_f32(*(volatile uint32_t *)&s_fmn[r]);
+            const float mxf = unord_f32(*(volatile uint32_t *)&s_fmx[r]);
+            if (!(y[r].h - slack > mnf) || !(y[r].h + slack < mxf)) return false;
         }
         return true;
     };
-    // after the f64 chain: f32 bounds of the thread's exact box
-    auto shadow = [&]() {
+    // after the f64 chain: the point's value bounds the block's box
+    auto certify = [&](const uint64_t *q) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-            const uint64_t a = mn[d], b = mx[d];
-            const uint64_t qa = (a & 0x8000000000000000ull) ? (a & 0x7fffffffffffffffull) : ~a;
-            const uint64_t qb = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
-            const float fa = f32_from_bits(f64bits_to_f32bits(qa)), fb = f32_from_bits(f64bits_to_f32bits(qb));
-            mnf[d] = isfinite(fa) ? f32_step(fa, 1) : INFINITY;     // >= the minimum
-            mxf[d] = isfinite(fb) ? f32_step(fb, -1) : -INFINITY;   // <= the maximum
+            if ((q[d] & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) continue;  // NaN: not in the box
+            const float f = f32_from_bits(f64bits_to_f32bits(q[d]));
+            if (!isfinite(f)) continue;
+            atomicMin(&s_fmn[d], ord_f32(f32_step(f, 1)));   // above the value
+            atomicMax(&s_fmx[d], ord_f32(f32_step(f, -1)));  // below it
         }
     };
     if (F2K && mfast && n > 0) {
-        // Seed the box with one exact point per thread, drawn across the
-        // whole input (an odd-multiplier hash of the thread's index), and
-        // merged over the block: its extremes start near the input's, so few
-        // points need the f64 chain for the box later.  Seeds are input
-        // points, so the box stays exact.
+        // the box starts from one exact point per thread, drawn across the
+        // whole input (an odd-multiplier hash of the thread's index), so its
+        // extremes start near the input's
+        if (threadIdx.x < 3) {
+            s_fmn[threadIdx.x] = ord_f32(INFINITY);
+            s_fmx[threadIdx.x] = ord_f32(-INFINITY);
+        }
+        __syncthreads();
         const uint64_t g = (uint64_t)blockIdx.x * BLOCK + threadIdx.x;
         uint64_t q[D];
         point(pts + ((g * 0x9E3779B97F4A7C15ull) % n) * D, q);
-        const int sl = threadIdx.x & 31, sw = threadIdx.x >> 5;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const uint64_t a = warp_min_u64(mn[d]), b = warp_max_u64(mx[d]);
-            if (sl == 0) {
-                red[2 * d][sw] = a;
-                red[2 * d + 1][sw] = b;
-            }
-        }
+        certify(q);
         __syncthreads();
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            for (int w2 = 0; w2 < NWARPS; ++w2) {
-                mn[d] = red[2 * d][w2] < mn[d] ? red[2 * d][w2] : mn[d];
-                mx[d] = red[2 * d + 1][w2] > mx[d] ? red[2 * d + 1][w2] : mx[d];
-            }
-        __syncthreads();  // red is written again at the end
-        shadow();
     }
     // Tiles of CONV_TILE points move to shared memory by asynchronous copies
     // (the next tile lands while this one is converted): consecutive threads
@@ -565,7 +549,6 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
 #pragma unroll
         for (int r = 0; r < CONV_TILE / BLOCK; ++r) {
             const uint32_t j = r * BLOCK + threadIdx.x;
-            bool exact = false;  // this lane evaluated the f64 chain
             if (j < np) {
                 if (multi && (p0 + j < cur.beg || p0 + j >= cur.end)) {
                     flush();
@@ -587,17 +570,8 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                     point(&tile[buf][j * D], q);
 #pragma unroll
                     for (int d = 0; d < D; ++d) outs[d][p0 + j] = KT::from_f64_bits(q[d]);
-                    exact = true;
+                    if (F2K && mfast) certify(q);
                 }
-            }
-            if (F2K && mfast && __any_sync(0xffffffffu, exact)) {
-                // the warp's box from its lanes' exact values
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    mn[d] = warp_min_u64(mn[d]);
-                    mx[d] = warp_max_u64(mx[d]);
-                }
-                shadow();
             }
         }
         __syncthreads();  // the buffer is free for the tile after next
