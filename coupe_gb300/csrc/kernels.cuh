@@ -490,6 +490,40 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
             atomicMax(&s_fmx[d], ord_f32(f32_step(f, -1)));  // below it
         }
     };
+    // F2K: the points that need the f64 chain wait in a per-warp queue (their
+    // coordinates and output position) and are evaluated 32 at a time, one
+    // per lane, so that the FP64 pipe runs whole warps instead of one lane
+    __shared__ double s_qp[F2K ? NWARPS : 1][F2K ? 64 : 1][3];
+    __shared__ uint64_t s_qi[F2K ? NWARPS : 1][F2K ? 64 : 1];
+    uint32_t qn = 0;  // entries in this warp's queue (the same in every lane)
+    auto drain = [&](uint32_t cnt) {  // the first cnt <= 32 entries; every lane calls it
+        const int ql = threadIdx.x & 31, qw = threadIdx.x >> 5;
+        __syncwarp();
+        if ((uint32_t)ql < cnt) {
+            uint64_t q[D];
+            point(&s_qp[qw][ql][0], q);
+            const uint64_t i = s_qi[qw][ql];
+#pragma unroll
+            for (int d = 0; d < D; ++d) outs[d][i] = KT::from_f64_bits(q[d]);
+            certify(q);
+        }
+        __syncwarp();
+        qn -= cnt;  // the rest (fewer than 32) moves to the front
+        double v[D];
+        uint64_t vi = 0;
+        if ((uint32_t)ql < qn) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) v[d] = s_qp[qw][cnt + ql][d];
+            vi = s_qi[qw][cnt + ql];
+        }
+        __syncwarp();
+        if ((uint32_t)ql < qn) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) s_qp[qw][ql][d] = v[d];
+            s_qi[qw][ql] = vi;
+        }
+        __syncwarp();
+    };
     if (F2K && mfast && n > 0) {
         // the box starts from one exact point per thread, drawn across the
         // whole input (an odd-multiplier hash of the thread's index), so its
@@ -549,6 +583,7 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
 #pragma unroll
         for (int r = 0; r < CONV_TILE / BLOCK; ++r) {
             const uint32_t j = r * BLOCK + threadIdx.x;
+            bool queue = false;  // F2K: this lane's point waits for the f64 chain
             if (j < np) {
                 if (multi && (p0 + j < cur.beg || p0 + j >= cur.end)) {
                     flush();
@@ -561,8 +596,10 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                         if (point_f2(&tile[buf][j * D], kk)) {
 #pragma unroll
                             for (int d = 0; d < D; ++d) outs[d][p0 + j] = kk[d];
-                            done = true;
+                        } else {
+                            queue = true;
                         }
+                        done = true;
                     }
                 }
                 if (!done) {
@@ -570,13 +607,25 @@ __global__ void __launch_bounds__(BLOCK) k_convert(const double *__restrict__ pt
                     point(&tile[buf][j * D], q);
 #pragma unroll
                     for (int d = 0; d < D; ++d) outs[d][p0 + j] = KT::from_f64_bits(q[d]);
-                    if (F2K && mfast) certify(q);
                 }
+            }
+            if (F2K && mfast) {
+                const int ql = threadIdx.x & 31, qw = threadIdx.x >> 5;
+                const uint32_t m = __ballot_sync(0xffffffffu, queue);
+                if (queue) {
+                    const uint32_t at = qn + __popc(m & ((1u << ql) - 1));
+#pragma unroll
+                    for (int d = 0; d < D; ++d) s_qp[qw][at][d] = tile[buf][j * D + d];
+                    s_qi[qw][at] = p0 + j;
+                }
+                qn += __popc(m);
+                if (qn >= 32) drain(32);
             }
         }
         __syncthreads();  // the buffer is free for the tile after next
         buf ^= 1;
     }
+    if (F2K && mfast && qn) drain(qn);
     if (multi) {
         flush();
         return;
