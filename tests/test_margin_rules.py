@@ -12,7 +12,8 @@
   * band_far (k_decide, band form): hi <= t + dist certainly false;
   * f2_split and the f32-pair Rib key and box shortcuts (point_f2 in
     k_convert): the key RN32 of coupe's f64 basis-change chain, and the box
-    of the mapped points, as the f64 chain gives them.
+    of the mapped points, as the f64 chain gives them;
+  * k_moments_f2: the f32-pair inertia sums against exactly rounded sums.
 
 Each replay asserts that whenever a shortcut decides, it decides as the
 exact expression does.  The GPU parity tests check the kernels end to end.
@@ -335,3 +336,44 @@ def test_rib_box_shortcut():
             mnf = np.nextafter(F32(mn), F32(np.inf))
             mxf = np.nextafter(F32(mx), F32(-np.inf))
         assert mn == y.min() and mx == y.max()
+
+
+def test_pair_inertia_sums_accuracy():
+    """k_moments_f2: the unweighted Rib sums (offsets from the first point,
+    their sums and products) in f32-pair arithmetic, one thread's sequence
+    at a time, match exactly rounded sums to 1e-12 relative."""
+    from math import fsum
+    mul, add = _pair_ops()
+    rng = np.random.default_rng(0)
+    side = 24
+    g = np.arange(side) + 0.5
+    x, y, z = np.meshgrid(g, g * 10, g * 100, indexing="ij")
+    q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+    pts = np.stack([x.ravel(), y.ravel(), z.ravel()], 1) @ q.T + 1000.0
+    s = [_f2_split(float(v)) for v in pts[0]]
+    pairs = [(a, b) for a in range(3) for b in range(a, 3)]
+    threads = 64
+    S1 = np.zeros(3)
+    S2 = np.zeros(len(pairs))
+    for t in range(threads):
+        a1 = [(F32(0), F32(0))] * 3
+        a2 = [(F32(0), F32(0))] * len(pairs)
+        for p in pts[t::threads]:
+            o = []
+            for d in range(3):
+                ph, pl = _f2_split(float(p[d]))
+                sh = F32(ph + F32(-s[d][0]))
+                v = F32(sh - ph)
+                err = F32(F32(ph - F32(sh - v)) + F32(F32(-s[d][0]) - v))
+                t2 = F32(err + F32(pl - s[d][1]))
+                hi = F32(sh + t2)
+                o.append((hi, F32(t2 - F32(hi - sh))))
+            a1 = [add(a1[d], o[d]) for d in range(3)]
+            a2 = [add(a2[k], mul(o[i], o[j])) for k, (i, j) in enumerate(pairs)]
+        S1 += [float(h) + float(l) for h, l in a1]
+        S2 += [float(h) + float(l) for h, l in a2]
+    off = pts - pts[0]
+    R1 = np.array([fsum(off[:, d]) for d in range(3)])
+    R2 = np.array([fsum(off[:, i] * off[:, j]) for i, j in pairs])
+    assert np.abs(S1 - R1).max() <= 1e-12 * np.abs(R1).max()
+    assert np.abs(S2 - R2).max() <= 1e-12 * np.abs(R2).max()
