@@ -268,6 +268,34 @@ def test_rib_with_given_matrix(coupe, oracle_mod):
     assert (want == got).all()
 
 
+@pytest.mark.parametrize("case", ["grid", "gauss"])
+def test_rib_2d_with_given_matrix(coupe, oracle_mod, case):
+    """2D Rib given the same basis change: REF32 ids equal the oracle's and
+    the band form's equal F64's (the f32-pair basis change of k_convert, a
+    rotated grid in index order included)."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(3)
+    if case == "grid":
+        g = np.arange(300) + 0.5
+        x, y = np.meshgrid(g, g * 10, indexing="ij")
+        th = 0.7
+        rot = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]])
+        pts = np.stack([x.ravel(), y.ravel()], 1) @ rot.T
+    else:
+        pts = rng.standard_normal((100_000, 2)) * [100.0, 3.0] + rng.standard_normal(2) * 50
+    w = rng.integers(1, 100, len(pts)).astype(np.int64)
+    M = oracle_mod.rib_matrix(pts)
+    want, _ = oracle_mod.rib(pts, w, 7, 0.01, matrix=M)
+    d_pts, d_w = torch.from_numpy(pts).cuda(), torch.from_numpy(w).cuda()
+    got = {}
+    for mode in ("ref32", "f64", "f32key_f64band"):
+        part = torch.empty(len(pts), dtype=torch.int64, device="cuda")
+        coupe.rcb_device(part, d_pts, d_w, 7, 0.01, matrix=M, mode=mode)
+        got[mode] = part.cpu().numpy().view(np.uint64)
+    assert (want == got["ref32"]).all()
+    assert (got["f64"] == got["f32key_f64band"]).all()
+
+
 def test_rib_matrix_matches_oracle(coupe, oracle_mod):
     torch = pytest.importorskip("torch")
     from coupe_gb300 import workloads
